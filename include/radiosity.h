@@ -1,0 +1,122 @@
+/* radiosity.h - C ABI of the GB300 progressive-refinement hemicube radiosity solver.
+ *
+ * Drop-in boundary for the reference's shoot loop (david-sabata/Radiosity,
+ * source/Main.cpp:1124-1309).  The reference has no FFI; its "API" is the set of
+ * C++ classes the loop calls.  Each entry point below names the reference code it
+ * replaces.  All calls return an int status (RAD_OK = 0, negative = error) and
+ * never throw or abort.  Host arrays are caller-owned and copied; device memory is
+ * owned by the rad_ctx.  A rad_ctx is not thread-safe: one context per host thread.
+ */
+#ifndef RADIOSITY_GB300_H
+#define RADIOSITY_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RAD_OK 0
+#define RAD_E_INVALID (-1)  /* bad argument (reference: cerr + ignore, source/Config.cpp:54-112) */
+#define RAD_E_CUDA (-2)     /* CUDA runtime error (reference: _ASSERT on CL calls) */
+#define RAD_E_OVERFLOW (-3) /* triangle or bin capacity exceeded; results of the call invalid */
+#define RAD_E_STATE (-4)    /* call out of order (e.g. no scene uploaded) */
+#define RAD_E_NOMEM (-5)    /* device allocation failed */
+#define RAD_E_TIMEOUT (-6)  /* a bounded device wait gave up */
+
+typedef enum { RAD_MODE_REF = 0, RAD_MODE_PHYS = 1 } rad_mode;
+
+/* Mirrors the static Config of source/Config.h:6-37 plus the solver's own knobs. */
+typedef struct rad_config {
+    uint32_t hemicube_side;   /* Config::setHemicubeSide (default 16); even, 2..2048 */
+    uint32_t ocl_workitems_x; /* Config::setOCLWorkitemsX (default 4); derived sizes only */
+    uint32_t shoots_per_cycle;/* Config::setShootsPerCycle (default 500) */
+    uint32_t hemicubes_count; /* Config::setHemicubesCount (default 10): shooters per batch K, 1..1024 */
+    double max_patch_area;    /* Config::setMaxPatchArea (default 0.5) */
+    uint32_t mode;            /* rad_mode: REF = the reference's update rule, PHYS = rho*F*Ai/Aj */
+    uint32_t tile;            /* raster bin side in pixels: 16, 32 or 64; 0 = choose by W */
+    double tolerance;         /* PHYS stop rule: unshot power / initial power <= tolerance */
+    uint32_t tri_capacity;    /* triangle records per hemicube; 0 = 2*N + 4096 */
+    uint32_t binref_capacity; /* bin references per hemicube; 0 = 4 * tri_capacity */
+    int32_t device;           /* CUDA device ordinal */
+} rad_config;
+
+typedef struct rad_stats {
+    uint32_t shots_done;   /* batches (reference "shoot" iterations) executed by the call */
+    uint32_t stopped;      /* 1 when the stop rule fired (source/Main.cpp:1298-1300) */
+    float last_energy[3];  /* REF: lastEnergy of source/Main.cpp:1287-1295 */
+    double residual;       /* PHYS: unshot power / initial power, FP64 sum */
+    double hemicubes;      /* hemicubes rendered by the call */
+    double device_ms;      /* device time of the call, CUDA events on the context stream */
+} rad_stats;
+
+typedef struct rad_ctx rad_ctx;
+
+/* Defaults of source/Config.cpp:6-10 (hemicube 16, work-items 4, 500 shots,
+ * area 0.5, 10 hemicubes), REF mode. */
+int rad_config_default(rad_config* cfg);
+
+/* Config::freeze derived values (source/Config.cpp:30-48): out[0..8] = HEMICUBE_W,
+ * HEMICUBE_H, PATCHVIEW_TEX_W, PATCHVIEW_TEX_H, PATCHVIEW_TEX_RES, OCL_WORKITEMS_X,
+ * OCL_WORKITEMS_Y, HEMICUBES_CNT, span length (source/Main.cpp:555). */
+int rad_config_derived(const rad_config* cfg, uint32_t out[9]);
+
+/* Creates a context on cfg->device: replaces InitGLObjects/InitCLObjects
+ * (source/Main.cpp:11-611).  *out is NULL on failure. */
+int rad_create(const rad_config* cfg, rad_ctx** out);
+
+/* Releases every device resource (CleanupGLObjects/CleanupCLObjects, source/Main.cpp:616-670). */
+int rad_destroy(rad_ctx* ctx);
+
+/* Uploads the scene of ModelContainer::getVertices/getIndices/getPatches
+ * (source/ModelContainer.cpp:135-209): vertices N*12 floats (4 corners per patch),
+ * indices N*6 (may be NULL; if given it must be the (0,1,2,0,2,3)+4i pattern),
+ * color N*3 (Patch::getColor), reflectance N*3 (PHYS only, may be NULL in REF),
+ * radiosity N*3 (Patch::radiosity = unshot energy), illumination N*3. */
+int rad_upload_scene(rad_ctx* ctx, const float* vertices, const int32_t* indices, const float* color,
+                     const float* reflectance, const float* radiosity, const float* illumination,
+                     uint32_t n);
+
+/* Replaces the radiosity / illumination state (either may be NULL to keep it). */
+int rad_set_state(rad_ctx* ctx, const float* radiosity, const float* illumination);
+
+/* Copies Patch::radiosity and Patch::illumination (N*3 each; either may be NULL). */
+int rad_download(rad_ctx* ctx, float* radiosity, float* illumination);
+
+/* precomputeHemicubeFormFactors (source/FormFactors.cpp:280-339): `copies` stacked
+ * texture-layout tables, 2W x 1.5W floats each, written to out. */
+int rad_ff_table(rad_ctx* ctx, float* out, uint32_t copies);
+
+/* ModelContainer::getHighestRadiosityPatchesId (source/ModelContainer.cpp:313-353) on
+ * the device-resident state: K ids and validity flags (valid[k]==0 <=> NULL emitter).
+ * PHYS mode selects the K largest unshot powers instead. */
+int rad_select_shooters(rad_ctx* ctx, uint32_t* ids, uint8_t* valid);
+
+/* Hemicube item buffers of `count` shooters (the 5-face draw of source/Main.cpp:1155-1198):
+ * count stacked 2W x 1.5W uint32 images, 0 = nothing, else patch index + 1. */
+int rad_render_item_buffers(rad_ctx* ctx, const uint32_t* shooters, uint32_t count, uint32_t* items);
+
+/* ProcessHemicube (source/Kernel_ProcessHemicube.h:9-70) plus the record accumulation
+ * of source/Main.cpp:1257-1269 on caller-given item buffers: count x N form factors. */
+int rad_reduce_item_buffers(rad_ctx* ctx, const uint32_t* items, uint32_t count, float* ff_rows);
+
+/* Render + reduce fused: count x N form-factor rows of the given shooters. */
+int rad_ff_rows(rad_ctx* ctx, const uint32_t* shooters, uint32_t count, float* ff_rows);
+
+/* Runs up to n_shots batches of the shoot loop (source/Main.cpp:1137-1309) on the
+ * device-resident state, K = hemicubes_count shooters per batch; stops early on the
+ * stop rule.  stats may be NULL. */
+int rad_shoot(rad_ctx* ctx, uint32_t n_shots, rad_stats* stats);
+
+/* Builds the reference scene (ModelContainer::load, source/ModelContainer.cpp:89-110,
+ * PrimitiveModel ROOM/ROOMCLOSURE/CUBE/BLOCK subdivided to max_patch_area).  Call with
+ * NULL arrays to get *n; then again with arrays of capacity >= *n patches. */
+int rad_scene_reference(double max_patch_area, uint32_t capacity, uint32_t* n, float* vertices,
+                        int32_t* indices, float* color, float* radiosity, float* illumination);
+
+const char* rad_strerror(int status);
+const char* rad_last_error(const rad_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

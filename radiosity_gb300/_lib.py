@@ -1,0 +1,249 @@
+"""ctypes binding of the C ABI in include/radiosity.h.
+
+This is the binding a Python caller of the reference-facing boundary uses; the
+library is always the in-tree CUDA build (radiosity_gb300/libradiosity_gb300.so).
+There is no fallback: if the library is missing or CUDA is unavailable, the
+calls fail with an exception.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+RAD_OK = 0
+RAD_E_INVALID = -1
+RAD_E_CUDA = -2
+RAD_E_OVERFLOW = -3
+RAD_E_STATE = -4
+RAD_E_NOMEM = -5
+RAD_E_TIMEOUT = -6
+MODE_REF, MODE_PHYS = 0, 1
+
+# Every symbol include/radiosity.h declares.
+EXPORTS = [
+    "rad_config_default", "rad_config_derived", "rad_create", "rad_destroy", "rad_upload_scene",
+    "rad_set_state", "rad_download", "rad_ff_table", "rad_select_shooters", "rad_render_item_buffers",
+    "rad_reduce_item_buffers", "rad_ff_rows", "rad_shoot", "rad_scene_reference", "rad_strerror",
+    "rad_last_error",
+]
+
+
+class RadConfig(ctypes.Structure):
+    _fields_ = [
+        ("hemicube_side", ctypes.c_uint32),
+        ("ocl_workitems_x", ctypes.c_uint32),
+        ("shoots_per_cycle", ctypes.c_uint32),
+        ("hemicubes_count", ctypes.c_uint32),
+        ("max_patch_area", ctypes.c_double),
+        ("mode", ctypes.c_uint32),
+        ("tile", ctypes.c_uint32),
+        ("tolerance", ctypes.c_double),
+        ("tri_capacity", ctypes.c_uint32),
+        ("binref_capacity", ctypes.c_uint32),
+        ("device", ctypes.c_int32),
+    ]
+
+
+class RadStats(ctypes.Structure):
+    _fields_ = [
+        ("shots_done", ctypes.c_uint32),
+        ("stopped", ctypes.c_uint32),
+        ("last_energy", ctypes.c_float * 3),
+        ("residual", ctypes.c_double),
+        ("hemicubes", ctypes.c_double),
+        ("device_ms", ctypes.c_double),
+    ]
+
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+
+_LIB = None
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Loads (building first if needed) the in-tree library."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if build_if_missing and not _build.up_to_date():
+        _build.build()
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run radiosity_gb300.build.build()")
+    L = ctypes.CDLL(LIB_PATH)
+    vp = ctypes.c_void_p
+    P = ctypes.POINTER
+    L.rad_config_default.argtypes = [P(RadConfig)]
+    L.rad_config_derived.argtypes = [P(RadConfig), _u32p]
+    L.rad_create.argtypes = [P(RadConfig), P(vp)]
+    L.rad_destroy.argtypes = [vp]
+    L.rad_upload_scene.argtypes = [vp, _f32p, vp, _f32p, vp, _f32p, _f32p, ctypes.c_uint32]
+    L.rad_set_state.argtypes = [vp, vp, vp]
+    L.rad_download.argtypes = [vp, vp, vp]
+    L.rad_ff_table.argtypes = [vp, _f32p, ctypes.c_uint32]
+    L.rad_select_shooters.argtypes = [vp, _u32p, _u8p]
+    L.rad_render_item_buffers.argtypes = [vp, _u32p, ctypes.c_uint32, _u32p]
+    L.rad_reduce_item_buffers.argtypes = [vp, _u32p, ctypes.c_uint32, _f32p]
+    L.rad_ff_rows.argtypes = [vp, _u32p, ctypes.c_uint32, _f32p]
+    L.rad_shoot.argtypes = [vp, ctypes.c_uint32, P(RadStats)]
+    L.rad_scene_reference.argtypes = [ctypes.c_double, ctypes.c_uint32, P(ctypes.c_uint32), vp, vp, vp, vp, vp]
+    L.rad_strerror.argtypes = [ctypes.c_int]
+    L.rad_strerror.restype = ctypes.c_char_p
+    L.rad_last_error.argtypes = [vp]
+    L.rad_last_error.restype = ctypes.c_char_p
+    for name in EXPORTS:
+        getattr(L, name).restype = getattr(L, name).restype if name in ("rad_strerror", "rad_last_error") \
+            else ctypes.c_int
+    _LIB = L
+    return L
+
+
+class RadError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"radiosity status {status}: {msg}")
+        self.status = status
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def reference_scene(max_patch_area: float) -> dict:
+    """rad_scene_reference: the reference Cornell scene subdivided to max_patch_area."""
+    L = load()
+    n = ctypes.c_uint32(0)
+    rc = L.rad_scene_reference(max_patch_area, 0, ctypes.byref(n), None, None, None, None, None)
+    if rc:
+        raise RadError(rc, "rad_scene_reference")
+    N = n.value
+    out = dict(vertices=np.zeros(12 * N, np.float32), indices=np.zeros(6 * N, np.int32),
+               color=np.zeros(3 * N, np.float32), radiosity=np.zeros(3 * N, np.float32),
+               illumination=np.zeros(3 * N, np.float32))
+    rc = L.rad_scene_reference(max_patch_area, N, ctypes.byref(n), _ptr(out["vertices"]), _ptr(out["indices"]),
+                               _ptr(out["color"]), _ptr(out["radiosity"]), _ptr(out["illumination"]))
+    if rc:
+        raise RadError(rc, "rad_scene_reference")
+    out["n"] = N
+    return out
+
+
+def default_config(**kw) -> RadConfig:
+    L = load()
+    cfg = RadConfig()
+    L.rad_config_default(ctypes.byref(cfg))
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+def derived(cfg: RadConfig) -> np.ndarray:
+    out = np.zeros(9, np.uint32)
+    load().rad_config_derived(ctypes.byref(cfg), out)
+    return out
+
+
+class Solver:
+    """One rad_ctx: a device-resident scene and its shoot loop."""
+
+    def __init__(self, cfg: RadConfig | None = None, **kw):
+        self.L = load()
+        self.cfg = cfg if cfg is not None else default_config(**kw)
+        h = ctypes.c_void_p()
+        rc = self.L.rad_create(ctypes.byref(self.cfg), ctypes.byref(h))
+        if rc:
+            raise RadError(rc, self.L.rad_strerror(rc).decode())
+        self.h = h
+        self.n = 0
+
+    def _check(self, rc: int, what: str):
+        if rc:
+            raise RadError(rc, f"{what}: {self.L.rad_last_error(self.h).decode()}")
+
+    def close(self):
+        if self.h:
+            self.L.rad_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def K(self) -> int:
+        return int(self.cfg.hemicubes_count)
+
+    @property
+    def W(self) -> int:
+        return int(self.cfg.hemicube_side)
+
+    def upload(self, vertices, color, radiosity, illumination, reflectance=None, indices=None):
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1)
+        n = v.size // 12
+        c = np.ascontiguousarray(color, np.float32).reshape(-1)
+        r = np.ascontiguousarray(radiosity, np.float32).reshape(-1)
+        i = np.ascontiguousarray(illumination, np.float32).reshape(-1)
+        rho = None if reflectance is None else np.ascontiguousarray(reflectance, np.float32).reshape(-1)
+        idx = None if indices is None else np.ascontiguousarray(indices, np.int32).reshape(-1)
+        self._check(self.L.rad_upload_scene(self.h, v, _ptr(idx), c, _ptr(rho), r, i, n), "rad_upload_scene")
+        self.n = n
+
+    def set_state(self, radiosity=None, illumination=None):
+        r = None if radiosity is None else np.ascontiguousarray(radiosity, np.float32).reshape(-1)
+        i = None if illumination is None else np.ascontiguousarray(illumination, np.float32).reshape(-1)
+        self._check(self.L.rad_set_state(self.h, _ptr(r), _ptr(i)), "rad_set_state")
+
+    def download(self):
+        r = np.zeros(3 * self.n, np.float32)
+        i = np.zeros(3 * self.n, np.float32)
+        self._check(self.L.rad_download(self.h, _ptr(r), _ptr(i)), "rad_download")
+        return r, i
+
+    def ff_table(self, copies: int = 1) -> np.ndarray:
+        out = np.zeros(3 * self.W * self.W * copies, np.float32)
+        self._check(self.L.rad_ff_table(self.h, out, copies), "rad_ff_table")
+        return out
+
+    def select(self):
+        ids = np.zeros(self.K, np.uint32)
+        valid = np.zeros(self.K, np.uint8)
+        self._check(self.L.rad_select_shooters(self.h, ids, valid), "rad_select_shooters")
+        return ids, valid.astype(bool)
+
+    def item_buffers(self, shooters) -> np.ndarray:
+        s = np.ascontiguousarray(shooters, np.uint32).reshape(-1)
+        out = np.zeros(s.size * 3 * self.W * self.W, np.uint32)
+        self._check(self.L.rad_render_item_buffers(self.h, s, s.size, out), "rad_render_item_buffers")
+        return out
+
+    def reduce_items(self, items, count: int) -> np.ndarray:
+        it = np.ascontiguousarray(items, np.uint32).reshape(-1)
+        out = np.zeros(count * self.n, np.float32)
+        self._check(self.L.rad_reduce_item_buffers(self.h, it, count, out), "rad_reduce_item_buffers")
+        return out.reshape(count, self.n)
+
+    def ff_rows(self, shooters) -> np.ndarray:
+        s = np.ascontiguousarray(shooters, np.uint32).reshape(-1)
+        out = np.zeros(s.size * self.n, np.float32)
+        self._check(self.L.rad_ff_rows(self.h, s, s.size, out), "rad_ff_rows")
+        return out.reshape(s.size, self.n)
+
+    def shoot(self, n_shots: int) -> RadStats:
+        st = RadStats()
+        self._check(self.L.rad_shoot(self.h, n_shots, ctypes.byref(st)), "rad_shoot")
+        return st

@@ -1,0 +1,575 @@
+// C ABI of the solver (include/radiosity.h): context, device memory, batch
+// sequencing and the CUDA-graph shoot loop.
+//
+// One rad_ctx owns one CUDA stream on one device.  A shoot batch is nine
+// stream-ordered operations (2 memsets, select, camera, setup, scan, fill,
+// raster+reduce, update, emitters); rad_shoot captures one batch into a CUDA
+// graph once per context and replays it, checking the device stop flag every
+// 32 batches.  Every kernel reads the device stop flag first, so batches after
+// the stop rule fired are no-ops and the result equals the reference's early exit.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/radiosity.h"
+#include "rad_internal.cuh"
+
+namespace rad {
+void launch_power0(const float4* rad, const float* area, uint32_t n, DevState* st, cudaStream_t s);
+}
+
+using namespace rad;
+
+namespace {
+
+struct BatchBuf {
+    Batch b{};
+    uint32_t cap_k = 0;
+    bool has_items = false;
+};
+
+}  // namespace
+
+struct rad_ctx {
+    rad_config cfg{};
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string err;
+    Geo geo{};
+    uint32_t n = 0;
+    float* d_verts = nullptr;
+    float4* d_color = nullptr;
+    float4* d_rho = nullptr;
+    float4* d_rad = nullptr;
+    float4* d_illum = nullptr;
+    float* d_area = nullptr;
+    float* d_fftab = nullptr;
+    BinInfo* d_bins = nullptr;
+    DevState* d_state = nullptr;   // shoot loop state
+    DevState* d_aux = nullptr;     // state for the one-off entry points
+    uint32_t* h_flag = nullptr;    // pinned stop flag
+    BatchBuf shoot;                // K = hemicubes_count
+    BatchBuf aux;                  // one-off calls, grown on demand
+    float* d_rows = nullptr;       // float rows for ff_rows / reduce
+    size_t rows_cap = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+};
+
+#define RAD_CUDA(ctx, call)                                                                         \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess) {                                                                    \
+            (ctx)->err = std::string(#call) + ": " + cudaGetErrorString(e_);                        \
+            return e_ == cudaErrorMemoryAllocation ? RAD_E_NOMEM : RAD_E_CUDA;                      \
+        }                                                                                           \
+    } while (0)
+
+static int fail(rad_ctx* ctx, int code, const char* msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+template <typename T>
+static void dfree(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+static void free_batch(BatchBuf& bb) {
+    dfree(bb.b.shooters);
+    dfree(bb.b.valid);
+    dfree(bb.b.saved);
+    dfree(bb.b.mvp);
+    dfree(bb.b.frame);
+    dfree(bb.b.tris);
+    dfree(bb.b.bin_count);
+    dfree(bb.b.bin_offset);
+    dfree(bb.b.bin_fill);
+    dfree(bb.b.bin_list);
+    dfree(bb.b.Fq);
+    dfree(bb.b.items);
+    bb.cap_k = 0;
+    bb.has_items = false;
+}
+
+static uint32_t tri_cap_per_hemi(const rad_ctx* c) {
+    return c->cfg.tri_capacity ? c->cfg.tri_capacity : 3u * c->n + 4096u;
+}
+static uint32_t list_cap_per_hemi(const rad_ctx* c) {
+    return c->cfg.binref_capacity ? c->cfg.binref_capacity : 4u * tri_cap_per_hemi(c);
+}
+
+static int alloc_batch(rad_ctx* c, BatchBuf& bb, uint32_t K, bool items) {
+    if (bb.cap_k >= K && (!items || bb.has_items) && bb.b.Fq) {
+        bb.b.K = K;
+        return RAD_OK;
+    }
+    free_batch(bb);
+    Batch& b = bb.b;
+    const uint64_t tri_cap = (uint64_t)tri_cap_per_hemi(c) * K, list_cap = (uint64_t)list_cap_per_hemi(c) * K;
+    if (tri_cap > 0xFFFFFFF0ull || list_cap > 0xFFFFFFF0ull)
+        return fail(c, RAD_E_INVALID, "batch capacity exceeds 2^32 records; lower hemicubes_count");
+    b.K = K;
+    b.tri_cap = (uint32_t)tri_cap;
+    b.list_cap = (uint32_t)list_cap;
+    const size_t nbk = (size_t)K * c->geo.nb;
+    RAD_CUDA(c, cudaMalloc(&b.shooters, sizeof(uint32_t) * K));
+    RAD_CUDA(c, cudaMalloc(&b.valid, sizeof(uint32_t) * K));
+    RAD_CUDA(c, cudaMalloc(&b.saved, sizeof(float4) * K));
+    RAD_CUDA(c, cudaMalloc(&b.mvp, sizeof(float) * 16 * 5 * K));
+    RAD_CUDA(c, cudaMalloc(&b.frame, sizeof(float) * 8 * K));
+    RAD_CUDA(c, cudaMalloc(&b.tris, sizeof(TriRec) * tri_cap));
+    RAD_CUDA(c, cudaMalloc(&b.bin_count, sizeof(uint32_t) * nbk));
+    RAD_CUDA(c, cudaMalloc(&b.bin_offset, sizeof(uint32_t) * nbk));
+    RAD_CUDA(c, cudaMalloc(&b.bin_fill, sizeof(uint32_t) * nbk));
+    RAD_CUDA(c, cudaMalloc(&b.bin_list, sizeof(uint32_t) * list_cap));
+    RAD_CUDA(c, cudaMalloc(&b.Fq, sizeof(unsigned long long) * (size_t)K * c->n));
+    RAD_CUDA(c, cudaMemsetAsync(b.Fq, 0, sizeof(unsigned long long) * (size_t)K * c->n, c->stream));
+    RAD_CUDA(c, cudaMemsetAsync(b.valid, 0, sizeof(uint32_t) * K, c->stream));
+    if (items) RAD_CUDA(c, cudaMalloc(&b.items, sizeof(uint32_t) * (size_t)K * c->geo.RES));
+    b.bins = c->d_bins;
+    bb.cap_k = K;
+    bb.has_items = items;
+    return RAD_OK;
+}
+
+static void drop_graph(rad_ctx* c) {
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    c->graph_exec = nullptr;
+    c->graph = nullptr;
+}
+
+static void setup_geo(rad_ctx* c, std::vector<BinInfo>& bins) {
+    Geo& g = c->geo;
+    const uint32_t W = c->cfg.hemicube_side;
+    g.W = W;
+    g.TW = 2 * W;
+    g.TH = (uint32_t)(W * 1.5);
+    g.RES = g.TW * g.TH;
+    g.mode = c->cfg.mode;
+    uint32_t tile = c->cfg.tile;
+    if (tile == 0) tile = W >= 512 ? 64 : (W >= 64 ? 32 : 16);
+    g.tile = tile;
+    const int w = (int)W, h = (int)W;
+    uint32_t base = 0;
+    bins.clear();
+    for (int f = 0; f < 5; f++) {
+        FaceInfo& F = g.face[f];
+        F.vp[2] = w;
+        F.vp[3] = h;
+        switch (f) {  // source/Main.cpp:316-389 with hemicube offset 0
+            case 0: F.vp[0] = 0; F.vp[1] = h; break;
+            case 1: F.vp[0] = w; F.vp[1] = h / 2; break;
+            case 2: F.vp[0] = -1 * (int)(W / 2); F.vp[1] = 0; break;
+            case 3: F.vp[0] = (int)(W * 1.5); F.vp[1] = 0; break;
+            default: F.vp[0] = w / 2; F.vp[1] = 0; break;
+        }
+        if (f == 0 || f == 1) {
+            F.sc[1] = h;
+            F.sc[3] = h / 2;
+        } else {
+            F.sc[1] = 0;
+            F.sc[3] = h;
+        }
+        F.sc[2] = (f == 2 || f == 3) ? w / 2 : w;
+        switch (f) {
+            case 0: case 2: F.sc[0] = 0; break;
+            case 1: F.sc[0] = w; break;
+            case 3: F.sc[0] = (int)(W * 1.5); break;
+            default: F.sc[0] = w / 2; break;
+        }
+        F.bins_x = (F.sc[2] + (int)tile - 1) / (int)tile;
+        F.bins_y = (F.sc[3] + (int)tile - 1) / (int)tile;
+        F.bin_base = (int)base;
+        for (int r = 0; r < F.bins_y; r++)
+            for (int cc = 0; cc < F.bins_x; cc++) {
+                BinInfo bi;
+                bi.x0 = (int16_t)(F.sc[0] + cc * (int)tile);
+                bi.y0 = (int16_t)(F.sc[1] + r * (int)tile);
+                bi.w = (int16_t)std::min((int)tile, F.sc[0] + F.sc[2] - bi.x0);
+                bi.h = (int16_t)std::min((int)tile, F.sc[1] + F.sc[3] - bi.y0);
+                bi.face = f;
+                bins.push_back(bi);
+            }
+        base += (uint32_t)(F.bins_x * F.bins_y);
+    }
+    g.nb = base;
+    // Perspective(90, 1.0, 0.01, 1000) -> Frustum (source/Transform.cpp:26-80, source/Main.cpp:1172)
+    const float PI = 3.1415926535897932384626433832795028841971691075f;
+    float fov = 90, aspect = 1.0f, zn = 0.01f, zf = 1000;
+    float fh = (float)(tanf(fov * PI / 180 * .5f)) * zn;
+    float fw = fh * aspect;
+    float l = -fw, r = fw, bt = -fh, t = fh;
+    float* p = g.proj;
+    p[0] = 2 * zn / (r - l); p[4] = 0; p[8] = (r + l) / (r - l); p[12] = 0;
+    p[1] = 0; p[5] = 2 * zn / (t - bt); p[9] = (t + bt) / (t - bt); p[13] = 0;
+    p[2] = 0; p[6] = 0; p[10] = -(zf + zn) / (zf - zn); p[14] = -2 * zf * zn / (zf - zn);
+    p[3] = 0; p[7] = 0; p[11] = -1; p[15] = 0;
+}
+
+static int check_cfg(const rad_config* cfg) {
+    if (!cfg) return RAD_E_INVALID;
+    const uint32_t W = cfg->hemicube_side;
+    if (W < 2 || W > 2048 || (W & 1u)) return RAD_E_INVALID;
+    if (cfg->hemicubes_count < 1 || cfg->hemicubes_count > (uint32_t)kMaxK) return RAD_E_INVALID;
+    if (cfg->tile != 0 && cfg->tile != 16 && cfg->tile != 32 && cfg->tile != 64) return RAD_E_INVALID;
+    if (cfg->mode > 1) return RAD_E_INVALID;
+    if (cfg->ocl_workitems_x == 0) return RAD_E_INVALID;
+    return RAD_OK;
+}
+
+// One shoot batch on the context stream (graph-capturable: no sync, no alloc).
+static void enqueue_batch(rad_ctx* c) {
+    Batch& b = c->shoot.b;
+    cudaStream_t s = c->stream;
+    cudaMemsetAsync(&c->d_state->tri_count, 0, sizeof(uint32_t), s);
+    cudaMemsetAsync(b.bin_count, 0, sizeof(uint32_t) * (size_t)b.K * c->geo.nb, s);
+    launch_select(c->geo, b, c->d_rad, c->d_area, c->d_state, s);
+    launch_camera(c->geo, b, c->d_verts, c->d_rad, c->d_state, s);
+    launch_setup(c->geo, b, c->d_verts, c->d_state, s);
+    launch_bins(c->geo, b, c->d_state, s);
+    launch_raster(c->geo, b, c->d_fftab, c->d_state, false, true, s);
+    launch_update(c->geo, b, c->d_color, c->d_rho, c->d_area, c->d_rad, c->d_state, s);
+    launch_emitters(c->geo, b, c->d_rad, c->d_illum, c->d_area, c->cfg.tolerance, nullptr, c->d_state, s);
+}
+
+// Render (and optionally reduce) `count` given shooters with the aux batch.
+static int run_aux(rad_ctx* c, const uint32_t* shooters, uint32_t count, bool items, bool fused) {
+    if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
+    if (!shooters || count == 0) return fail(c, RAD_E_INVALID, "no shooters");
+    for (uint32_t i = 0; i < count; i++)
+        if (shooters[i] >= c->n) return fail(c, RAD_E_INVALID, "shooter index out of range");
+    int rc = alloc_batch(c, c->aux, count, items);
+    if (rc) return rc;
+    Batch& b = c->aux.b;
+    b.K = count;
+    cudaStream_t s = c->stream;
+    std::vector<uint32_t> ones(count, 1u);
+    RAD_CUDA(c, cudaMemsetAsync(c->d_aux, 0, sizeof(DevState), s));
+    RAD_CUDA(c, cudaMemcpyAsync(b.shooters, shooters, sizeof(uint32_t) * count, cudaMemcpyHostToDevice, s));
+    RAD_CUDA(c, cudaMemcpyAsync(b.valid, ones.data(), sizeof(uint32_t) * count, cudaMemcpyHostToDevice, s));
+    RAD_CUDA(c, cudaMemsetAsync(b.bin_count, 0, sizeof(uint32_t) * (size_t)count * c->geo.nb, s));
+    RAD_CUDA(c, cudaMemsetAsync(b.Fq, 0, sizeof(unsigned long long) * (size_t)count * c->n, s));
+    launch_camera(c->geo, b, c->d_verts, c->d_rad, c->d_aux, s);
+    launch_setup(c->geo, b, c->d_verts, c->d_aux, s);
+    launch_bins(c->geo, b, c->d_aux, s);
+    launch_raster(c->geo, b, c->d_fftab, c->d_aux, items, fused, s);
+    RAD_CUDA(c, cudaGetLastError());
+    DevState st;
+    RAD_CUDA(c, cudaMemcpyAsync(&st, c->d_aux, sizeof(st), cudaMemcpyDeviceToHost, s));
+    RAD_CUDA(c, cudaStreamSynchronize(s));
+    if (st.overflow) return fail(c, RAD_E_OVERFLOW, "triangle or bin capacity exceeded");
+    return RAD_OK;
+}
+
+static int ensure_rows(rad_ctx* c, size_t count) {
+    if (c->rows_cap >= count) return RAD_OK;
+    dfree(c->d_rows);
+    RAD_CUDA(c, cudaMalloc(&c->d_rows, sizeof(float) * count));
+    c->rows_cap = count;
+    return RAD_OK;
+}
+
+extern "C" {
+
+int rad_config_default(rad_config* cfg) {
+    if (!cfg) return RAD_E_INVALID;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->hemicube_side = 16;      // source/Config.cpp:6-10
+    cfg->ocl_workitems_x = 4;
+    cfg->shoots_per_cycle = 500;
+    cfg->max_patch_area = 0.5;
+    cfg->hemicubes_count = 10;
+    cfg->mode = RAD_MODE_REF;
+    cfg->tile = 0;
+    cfg->tolerance = 0.0;
+    cfg->device = 0;
+    return RAD_OK;
+}
+
+int rad_config_derived(const rad_config* cfg, uint32_t out[9]) {
+    if (!cfg || !out) return RAD_E_INVALID;
+    const uint32_t W = cfg->hemicube_side, K = cfg->hemicubes_count;
+    out[0] = W;
+    out[1] = W;
+    out[2] = (uint32_t)(W * 2);
+    out[3] = (uint32_t)(W * 1.5);
+    out[4] = out[2] * out[3];
+    out[5] = std::min(cfg->ocl_workitems_x, out[2]);
+    out[6] = out[3] * K;
+    out[7] = K;
+    out[8] = out[5] ? out[2] / out[5] : 0;
+    return RAD_OK;
+}
+
+int rad_create(const rad_config* cfg, rad_ctx** out) {
+    if (!out) return RAD_E_INVALID;
+    *out = nullptr;
+    if (check_cfg(cfg) != RAD_OK) return RAD_E_INVALID;
+    rad_ctx* c = new rad_ctx();
+    c->cfg = *cfg;
+    int rc = RAD_OK;
+    auto bail = [&](int code) {
+        rad_destroy(c);
+        return code;
+    };
+    if (cudaSetDevice(cfg->device) != cudaSuccess) return bail(RAD_E_CUDA);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(RAD_E_CUDA);
+    if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) return bail(RAD_E_CUDA);
+    std::vector<BinInfo> bins;
+    setup_geo(c, bins);
+    if (cudaMalloc(&c->d_bins, sizeof(BinInfo) * bins.size()) != cudaSuccess) return bail(RAD_E_NOMEM);
+    if (cudaMemcpy(c->d_bins, bins.data(), sizeof(BinInfo) * bins.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(RAD_E_CUDA);
+    if (cudaMalloc(&c->d_fftab, sizeof(float) * c->geo.RES) != cudaSuccess) return bail(RAD_E_NOMEM);
+    if (cudaMalloc(&c->d_state, sizeof(DevState)) != cudaSuccess) return bail(RAD_E_NOMEM);
+    if (cudaMalloc(&c->d_aux, sizeof(DevState)) != cudaSuccess) return bail(RAD_E_NOMEM);
+    if (cudaMallocHost(&c->h_flag, sizeof(uint32_t)) != cudaSuccess) return bail(RAD_E_NOMEM);
+    cudaMemsetAsync(c->d_state, 0, sizeof(DevState), c->stream);
+    cudaMemsetAsync(c->d_aux, 0, sizeof(DevState), c->stream);
+    launch_fftab(c->geo.W, c->d_fftab, c->stream);
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(c->stream) != cudaSuccess) return bail(RAD_E_CUDA);
+    (void)rc;
+    *out = c;
+    return RAD_OK;
+}
+
+int rad_destroy(rad_ctx* c) {
+    if (!c) return RAD_E_INVALID;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    drop_graph(c);
+    free_batch(c->shoot);
+    free_batch(c->aux);
+    dfree(c->d_verts);
+    dfree(c->d_color);
+    dfree(c->d_rho);
+    dfree(c->d_rad);
+    dfree(c->d_illum);
+    dfree(c->d_area);
+    dfree(c->d_fftab);
+    dfree(c->d_bins);
+    dfree(c->d_state);
+    dfree(c->d_aux);
+    dfree(c->d_rows);
+    if (c->h_flag) cudaFreeHost(c->h_flag);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return RAD_OK;
+}
+
+static int upload_f3(rad_ctx* c, float4* dst, const float* src, uint32_t n) {
+    std::vector<float4> tmp(n);
+    for (uint32_t i = 0; i < n; i++)
+        tmp[i] = src ? make_float4(src[3 * i], src[3 * i + 1], src[3 * i + 2], 0.f) : make_float4(0, 0, 0, 0);
+    RAD_CUDA(c, cudaMemcpy(dst, tmp.data(), sizeof(float4) * n, cudaMemcpyHostToDevice));
+    return RAD_OK;
+}
+
+int rad_upload_scene(rad_ctx* c, const float* vertices, const int32_t* indices, const float* color,
+                     const float* reflectance, const float* radiosity, const float* illumination, uint32_t n) {
+    if (!c) return RAD_E_INVALID;
+    if (!vertices || !color || !radiosity || !illumination || n == 0)
+        return fail(c, RAD_E_INVALID, "vertices, color, radiosity and illumination are required");
+    if (c->cfg.mode == RAD_MODE_PHYS && !reflectance) return fail(c, RAD_E_INVALID, "PHYS mode needs reflectance");
+    if (n > 0x7FFFFFFFu) return fail(c, RAD_E_INVALID, "too many patches");
+    if (indices)
+        for (uint32_t i = 0; i < n; i++) {
+            const int32_t b = (int32_t)(4 * i);
+            const int32_t* q = indices + 6 * (size_t)i;
+            if (q[0] != b || q[1] != b + 1 || q[2] != b + 2 || q[3] != b || q[4] != b + 2 || q[5] != b + 3)
+                return fail(c, RAD_E_INVALID, "indices must follow the (0,1,2,0,2,3)+4i quad pattern");
+        }
+    cudaStreamSynchronize(c->stream);
+    drop_graph(c);
+    free_batch(c->shoot);
+    free_batch(c->aux);
+    dfree(c->d_verts);
+    dfree(c->d_color);
+    dfree(c->d_rho);
+    dfree(c->d_rad);
+    dfree(c->d_illum);
+    dfree(c->d_area);
+    c->n = n;
+    c->geo.n = n;
+    RAD_CUDA(c, cudaMalloc(&c->d_verts, sizeof(float) * 12 * (size_t)n));
+    RAD_CUDA(c, cudaMalloc(&c->d_color, sizeof(float4) * n));
+    RAD_CUDA(c, cudaMalloc(&c->d_rho, sizeof(float4) * n));
+    RAD_CUDA(c, cudaMalloc(&c->d_rad, sizeof(float4) * n));
+    RAD_CUDA(c, cudaMalloc(&c->d_illum, sizeof(float4) * n));
+    RAD_CUDA(c, cudaMalloc(&c->d_area, sizeof(float) * n));
+    RAD_CUDA(c, cudaMemcpy(c->d_verts, vertices, sizeof(float) * 12 * (size_t)n, cudaMemcpyHostToDevice));
+    int rc;
+    if ((rc = upload_f3(c, c->d_color, color, n))) return rc;
+    if ((rc = upload_f3(c, c->d_rho, reflectance, n))) return rc;
+    if ((rc = upload_f3(c, c->d_rad, radiosity, n))) return rc;
+    if ((rc = upload_f3(c, c->d_illum, illumination, n))) return rc;
+    launch_areas(c->d_verts, n, c->d_area, c->stream);
+    RAD_CUDA(c, cudaMemsetAsync(c->d_state, 0, sizeof(DevState), c->stream));
+    launch_power0(c->d_rad, c->d_area, n, c->d_state, c->stream);
+    RAD_CUDA(c, cudaGetLastError());
+    if ((rc = alloc_batch(c, c->shoot, c->cfg.hemicubes_count, false))) return rc;
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    return RAD_OK;
+}
+
+int rad_set_state(rad_ctx* c, const float* radiosity, const float* illumination) {
+    if (!c) return RAD_E_INVALID;
+    if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
+    cudaStreamSynchronize(c->stream);
+    int rc;
+    if (radiosity && (rc = upload_f3(c, c->d_rad, radiosity, c->n))) return rc;
+    if (illumination && (rc = upload_f3(c, c->d_illum, illumination, c->n))) return rc;
+    uint32_t zero = 0;
+    RAD_CUDA(c, cudaMemcpy(&c->d_state->stopped, &zero, sizeof(zero), cudaMemcpyHostToDevice));
+    return RAD_OK;
+}
+
+int rad_download(rad_ctx* c, float* radiosity, float* illumination) {
+    if (!c) return RAD_E_INVALID;
+    if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
+    std::vector<float4> tmp(c->n);
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    float* dst[2] = {radiosity, illumination};
+    float4* src[2] = {c->d_rad, c->d_illum};
+    for (int k = 0; k < 2; k++) {
+        if (!dst[k]) continue;
+        RAD_CUDA(c, cudaMemcpy(tmp.data(), src[k], sizeof(float4) * c->n, cudaMemcpyDeviceToHost));
+        for (uint32_t i = 0; i < c->n; i++) {
+            dst[k][3 * i] = tmp[i].x;
+            dst[k][3 * i + 1] = tmp[i].y;
+            dst[k][3 * i + 2] = tmp[i].z;
+        }
+    }
+    return RAD_OK;
+}
+
+int rad_ff_table(rad_ctx* c, float* out, uint32_t copies) {
+    if (!c || !out || copies == 0) return RAD_E_INVALID;
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    RAD_CUDA(c, cudaMemcpy(out, c->d_fftab, sizeof(float) * c->geo.RES, cudaMemcpyDeviceToHost));
+    for (uint32_t k = 1; k < copies; k++) std::memcpy(out + (size_t)k * c->geo.RES, out, sizeof(float) * c->geo.RES);
+    return RAD_OK;
+}
+
+int rad_select_shooters(rad_ctx* c, uint32_t* ids, uint8_t* valid) {
+    if (!c || !ids || !valid) return RAD_E_INVALID;
+    if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
+    Batch& b = c->shoot.b;
+    RAD_CUDA(c, cudaMemsetAsync(c->d_aux, 0, sizeof(DevState), c->stream));
+    launch_select(c->geo, b, c->d_rad, c->d_area, c->d_aux, c->stream);
+    RAD_CUDA(c, cudaGetLastError());
+    std::vector<uint32_t> v(b.K);
+    RAD_CUDA(c, cudaMemcpyAsync(ids, b.shooters, sizeof(uint32_t) * b.K, cudaMemcpyDeviceToHost, c->stream));
+    RAD_CUDA(c, cudaMemcpyAsync(v.data(), b.valid, sizeof(uint32_t) * b.K, cudaMemcpyDeviceToHost, c->stream));
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (uint32_t k = 0; k < b.K; k++) valid[k] = v[k] ? 1 : 0;
+    return RAD_OK;
+}
+
+int rad_render_item_buffers(rad_ctx* c, const uint32_t* shooters, uint32_t count, uint32_t* items) {
+    if (!c || !items) return RAD_E_INVALID;
+    int rc = run_aux(c, shooters, count, true, false);
+    if (rc) return rc;
+    RAD_CUDA(c, cudaMemcpy(items, c->aux.b.items, sizeof(uint32_t) * (size_t)count * c->geo.RES,
+                           cudaMemcpyDeviceToHost));
+    return RAD_OK;
+}
+
+int rad_reduce_item_buffers(rad_ctx* c, const uint32_t* items, uint32_t count, float* ff_rows) {
+    if (!c || !items || !ff_rows || count == 0) return RAD_E_INVALID;
+    if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
+    int rc = alloc_batch(c, c->aux, count, true);
+    if (rc) return rc;
+    if ((rc = ensure_rows(c, (size_t)count * c->n))) return rc;
+    Batch& b = c->aux.b;
+    b.K = count;
+    RAD_CUDA(c, cudaMemcpyAsync(b.items, items, sizeof(uint32_t) * (size_t)count * c->geo.RES,
+                                cudaMemcpyHostToDevice, c->stream));
+    RAD_CUDA(c, cudaMemsetAsync(b.Fq, 0, sizeof(unsigned long long) * (size_t)count * c->n, c->stream));
+    launch_reduce_items(c->geo, b, c->d_fftab, count, c->stream);
+    launch_fq_to_float(c->geo, b, count, c->d_rows, c->stream);
+    RAD_CUDA(c, cudaGetLastError());
+    RAD_CUDA(c, cudaMemcpyAsync(ff_rows, c->d_rows, sizeof(float) * (size_t)count * c->n, cudaMemcpyDeviceToHost,
+                                c->stream));
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    return RAD_OK;
+}
+
+int rad_ff_rows(rad_ctx* c, const uint32_t* shooters, uint32_t count, float* ff_rows) {
+    if (!c || !ff_rows) return RAD_E_INVALID;
+    int rc = run_aux(c, shooters, count, false, true);
+    if (rc) return rc;
+    if ((rc = ensure_rows(c, (size_t)count * c->n))) return rc;
+    launch_fq_to_float(c->geo, c->aux.b, count, c->d_rows, c->stream);
+    RAD_CUDA(c, cudaGetLastError());
+    RAD_CUDA(c, cudaMemcpyAsync(ff_rows, c->d_rows, sizeof(float) * (size_t)count * c->n, cudaMemcpyDeviceToHost,
+                                c->stream));
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    return RAD_OK;
+}
+
+int rad_shoot(rad_ctx* c, uint32_t n_shots, rad_stats* stats) {
+    if (!c) return RAD_E_INVALID;
+    if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
+    DevState before;
+    RAD_CUDA(c, cudaMemcpyAsync(&before, c->d_state, sizeof(before), cudaMemcpyDeviceToHost, c->stream));
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (!c->graph_exec) {
+        RAD_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_batch(c);
+        cudaError_t e = cudaStreamEndCapture(c->stream, &c->graph);
+        if (e != cudaSuccess) return fail(c, RAD_E_CUDA, cudaGetErrorString(e));
+        RAD_CUDA(c, cudaGraphInstantiate(&c->graph_exec, c->graph, 0));
+    }
+    RAD_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    for (uint32_t s = 0; s < n_shots; s++) {
+        RAD_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
+        if ((s & 31u) == 31u && s + 1 < n_shots) {
+            RAD_CUDA(c, cudaMemcpyAsync(c->h_flag, &c->d_state->stopped, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                        c->stream));
+            RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+            if (*c->h_flag) break;
+        }
+    }
+    RAD_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    DevState after;
+    RAD_CUDA(c, cudaMemcpyAsync(&after, c->d_state, sizeof(after), cudaMemcpyDeviceToHost, c->stream));
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    if (stats) {
+        stats->shots_done = after.shots_done - before.shots_done;
+        stats->stopped = after.stopped;
+        std::memcpy(stats->last_energy, after.last_energy, sizeof(float) * 3);
+        stats->residual = after.residual;
+        stats->hemicubes = after.hemicubes - before.hemicubes;
+        stats->device_ms = ms;
+    }
+    if (after.overflow) return fail(c, RAD_E_OVERFLOW, "triangle or bin capacity exceeded");
+    return RAD_OK;
+}
+
+const char* rad_strerror(int status) {
+    switch (status) {
+        case RAD_OK: return "ok";
+        case RAD_E_INVALID: return "invalid argument";
+        case RAD_E_CUDA: return "CUDA error";
+        case RAD_E_OVERFLOW: return "triangle or bin capacity exceeded";
+        case RAD_E_STATE: return "call out of order";
+        case RAD_E_NOMEM: return "device allocation failed";
+        case RAD_E_TIMEOUT: return "bounded device wait gave up";
+        default: return "unknown status";
+    }
+}
+
+const char* rad_last_error(const rad_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+}  // extern "C"

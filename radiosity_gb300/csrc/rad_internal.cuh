@@ -1,0 +1,110 @@
+// Internal types shared by the solver's translation units.
+//
+// Device data layout (one rad_ctx, all resident in HBM):
+//   scene      verts   float[N*12]  4 corners per patch, as ModelContainer::getVertices
+//              color   float4[N]    rgb of Patch::getColor
+//              rho     float4[N]    per-channel reflectance (PHYS)
+//              area    float[N]     quad area (PHYS)
+//              rad     float4[N]    Patch::radiosity   (unshot energy)
+//              illum   float4[N]    Patch::illumination (shot energy)
+//   hemicube   fftab   float[3W^2]  delta form factors, texture layout, ONE copy
+//   batch (K)  shooters/valid/saved/mvp/frame, triangle records, per-bin lists,
+//              Fq uint64[K*N] exact form-factor sums, optional item buffers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace rad {
+
+constexpr float kGuard = 1024.0f;       // guard-band clip |x|,|y| <= 1024 w
+constexpr float kReflectivity = 0.3f;   // REFLECTIVITY, source/Patch.h:13
+constexpr uint32_t kDeadTri = 0xFFFFFFFFu;
+constexpr int kMaxK = 1024;
+
+// One rasterisable triangle, hemicube-local 24.8 fixed-point window coordinates.
+struct __align__(16) TriRec {
+    int32_t X0, Y0, X1, Y1, X2, Y2;
+    float c0, ax, ay;       // depth (1/w) plane: D = (c0 + ax*(px-sx)) + ay*(py-sy)
+    uint32_t id;            // patch index, kDeadTri for an unused slot
+    int16_t px0, px1, py0, py1;  // pixel bbox clamped to the face scissor
+    uint32_t hf;            // hi*5 + face
+    uint32_t pad[3];
+};
+static_assert(sizeof(TriRec) == 64, "TriRec layout");
+
+struct BinInfo {
+    int16_t x0, y0, w, h;   // hemicube-local pixel rectangle
+    int32_t face;
+};
+
+struct FaceInfo {
+    int vp[4];              // viewport x,y,w,h (hemicube-local)
+    int sc[4];              // scissor x,y,w,h (hemicube-local)
+    int bin_base, bins_x, bins_y, pad;
+};
+
+// Per-context constants passed by value to kernels.
+struct Geo {
+    uint32_t W, TW, TH, RES;   // W, 2W, 1.5W, 3W^2
+    uint32_t n;                // patches
+    uint32_t nb;               // bins per hemicube
+    uint32_t tile;             // bin side
+    uint32_t mode;             // rad_mode
+    FaceInfo face[5];
+    float proj[16];            // Perspective(90,1,0.01,1000), column-major
+};
+
+// Device-side loop state (one per context).
+struct DevState {
+    uint32_t stopped;
+    uint32_t shots_done;
+    uint32_t overflow;
+    uint32_t tri_count;
+    float last_energy[4];
+    double residual;
+    double power0;
+    double hemicubes;
+    uint32_t timeouts;
+    uint32_t pad[3];
+};
+
+// Device pointers of one batch of K hemicubes.
+struct Batch {
+    uint32_t K;
+    uint32_t tri_cap;
+    uint32_t list_cap;
+    uint32_t pad;
+    uint32_t* shooters;          // K
+    uint32_t* valid;             // K
+    float4* saved;               // K
+    float* mvp;                  // K*5*16
+    float* frame;                // K*8 (center xyz, normal xyz)
+    TriRec* tris;                // tri_cap
+    uint32_t* bin_count;         // K*nb
+    uint32_t* bin_offset;        // K*nb
+    uint32_t* bin_fill;          // K*nb
+    uint32_t* bin_list;          // list_cap
+    unsigned long long* Fq;      // K*N exact sums (scale 2^61)
+    uint32_t* items;             // K*RES or null
+    const BinInfo* bins;         // nb
+};
+
+// Launchers (raster.cu / shoot.cu).  All run on `s`.
+void launch_camera(const Geo& g, const Batch& b, const float* verts, const float4* rad, DevState* st,
+                   cudaStream_t s);
+void launch_setup(const Geo& g, const Batch& b, const float* verts, DevState* st, cudaStream_t s);
+void launch_bins(const Geo& g, const Batch& b, DevState* st, cudaStream_t s);
+void launch_raster(const Geo& g, const Batch& b, const float* fftab, DevState* st, bool write_items,
+                   bool fused_reduce, cudaStream_t s);
+void launch_reduce_items(const Geo& g, const Batch& b, const float* fftab, uint32_t count, cudaStream_t s);
+void launch_fq_to_float(const Geo& g, const Batch& b, uint32_t count, float* out, cudaStream_t s);
+void launch_select(const Geo& g, const Batch& b, const float4* rad, const float* area, DevState* st,
+                   cudaStream_t s);
+void launch_update(const Geo& g, const Batch& b, const float4* color, const float4* rho, const float* area,
+                   float4* rad, DevState* st, cudaStream_t s);
+void launch_emitters(const Geo& g, const Batch& b, float4* rad, float4* illum, const float* area,
+                     double tol, double* partials, DevState* st, cudaStream_t s);
+void launch_areas(const float* verts, uint32_t n, float* area, cudaStream_t s);
+void launch_fftab(uint32_t W, float* fftab, cudaStream_t s);
+
+}  // namespace rad
