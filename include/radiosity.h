@@ -107,6 +107,22 @@ int rad_ff_rows(rad_ctx* ctx, const uint32_t* shooters, uint32_t count, float* f
  * stop rule.  stats may be NULL. */
 int rad_shoot(rad_ctx* ctx, uint32_t n_shots, rad_stats* stats);
 
+/* Stages of one shoot batch, in launch order (rad_profile_stages). */
+#define RAD_STAGE_SELECT 0   /* shooter selection (1 kernel) */
+#define RAD_STAGE_CAMERA 1   /* face MVPs + saved energy (1 kernel) */
+#define RAD_STAGE_SETUP 2    /* triangle setup + bin counts (1 kernel) */
+#define RAD_STAGE_BINS 3     /* bin scan + fill (2 kernels) */
+#define RAD_STAGE_RASTER 4   /* tile raster + fused delta-FF reduction (1 kernel) */
+#define RAD_STAGE_UPDATE 5   /* radiosity update (1 kernel) */
+#define RAD_STAGE_EMITTERS 6 /* emitters + stop rule (1 kernel) */
+#define RAD_N_STAGES 7
+
+/* Diagnostic twin of rad_shoot: runs up to n_shots batches launched stage by stage
+ * (no CUDA graph) with CUDA events between stages on the context stream and adds
+ * each stage's device milliseconds to stage_ms[RAD_N_STAGES] (caller zeroes it).
+ * The state advances exactly as with rad_shoot.  stats may be NULL. */
+int rad_profile_stages(rad_ctx* ctx, uint32_t n_shots, double* stage_ms, rad_stats* stats);
+
 /* Builds the reference scene (ModelContainer::load, source/ModelContainer.cpp:89-110,
  * PrimitiveModel ROOM/ROOMCLOSURE/CUBE/BLOCK subdivided to max_patch_area).  Call with
  * NULL arrays to get *n; then again with arrays of capacity >= *n patches. */

@@ -29,9 +29,11 @@ MODE_REF, MODE_PHYS = 0, 1
 EXPORTS = [
     "rad_config_default", "rad_config_derived", "rad_create", "rad_destroy", "rad_upload_scene",
     "rad_set_state", "rad_download", "rad_ff_table", "rad_select_shooters", "rad_render_item_buffers",
-    "rad_reduce_item_buffers", "rad_ff_rows", "rad_shoot", "rad_scene_reference", "rad_strerror",
-    "rad_last_error",
+    "rad_reduce_item_buffers", "rad_ff_rows", "rad_shoot", "rad_profile_stages", "rad_scene_reference",
+    "rad_strerror", "rad_last_error",
 ]
+STAGES = ["select", "camera", "setup", "bins", "raster", "update", "emitters"]
+STAGE_KERNELS = [1, 1, 1, 2, 1, 1, 1]
 
 
 class RadConfig(ctypes.Structure):
@@ -94,6 +96,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rad_reduce_item_buffers.argtypes = [vp, _u32p, ctypes.c_uint32, _f32p]
     L.rad_ff_rows.argtypes = [vp, _u32p, ctypes.c_uint32, _f32p]
     L.rad_shoot.argtypes = [vp, ctypes.c_uint32, P(RadStats)]
+    L.rad_profile_stages.argtypes = [vp, ctypes.c_uint32, np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS"),
+                                     P(RadStats)]
     L.rad_scene_reference.argtypes = [ctypes.c_double, ctypes.c_uint32, P(ctypes.c_uint32), vp, vp, vp, vp, vp]
     L.rad_strerror.argtypes = [ctypes.c_int]
     L.rad_strerror.restype = ctypes.c_char_p
@@ -242,6 +246,13 @@ class Solver:
         out = np.zeros(s.size * self.n, np.float32)
         self._check(self.L.rad_ff_rows(self.h, s, s.size, out), "rad_ff_rows")
         return out.reshape(s.size, self.n)
+
+    def profile_stages(self, n_shots: int):
+        """Per-stage device milliseconds (summed over the batches) and the stats."""
+        ms = np.zeros(len(STAGES), np.float64)
+        st = RadStats()
+        self._check(self.L.rad_profile_stages(self.h, n_shots, ms, ctypes.byref(st)), "rad_profile_stages")
+        return dict(zip(STAGES, ms.tolist())), st
 
     def shoot(self, n_shots: int) -> RadStats:
         st = RadStats()

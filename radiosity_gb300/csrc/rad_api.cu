@@ -557,6 +557,60 @@ int rad_shoot(rad_ctx* c, uint32_t n_shots, rad_stats* stats) {
     return RAD_OK;
 }
 
+int rad_profile_stages(rad_ctx* c, uint32_t n_shots, double* stage_ms, rad_stats* stats) {
+    if (!c || !stage_ms) return RAD_E_INVALID;
+    if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
+    Batch& b = c->shoot.b;
+    cudaStream_t s = c->stream;
+    cudaEvent_t ev[RAD_N_STAGES + 1];
+    for (auto& e : ev) RAD_CUDA(c, cudaEventCreate(&e));
+    DevState before;
+    RAD_CUDA(c, cudaMemcpyAsync(&before, c->d_state, sizeof(before), cudaMemcpyDeviceToHost, s));
+    RAD_CUDA(c, cudaStreamSynchronize(s));
+    float total_ms = 0;
+    for (uint32_t shot = 0; shot < n_shots; shot++) {
+        RAD_CUDA(c, cudaMemsetAsync(&c->d_state->tri_count, 0, sizeof(uint32_t), s));
+        RAD_CUDA(c, cudaMemsetAsync(b.bin_count, 0, sizeof(uint32_t) * (size_t)b.K * c->geo.nb, s));
+        RAD_CUDA(c, cudaEventRecord(ev[0], s));
+        launch_select(c->geo, b, c->d_rad, c->d_area, c->d_state, s);
+        RAD_CUDA(c, cudaEventRecord(ev[1], s));
+        launch_camera(c->geo, b, c->d_verts, c->d_rad, c->d_state, s);
+        RAD_CUDA(c, cudaEventRecord(ev[2], s));
+        launch_setup(c->geo, b, c->d_verts, c->d_state, s);
+        RAD_CUDA(c, cudaEventRecord(ev[3], s));
+        launch_bins(c->geo, b, c->d_state, s);
+        RAD_CUDA(c, cudaEventRecord(ev[4], s));
+        launch_raster(c->geo, b, c->d_fftab, c->d_state, false, true, s);
+        RAD_CUDA(c, cudaEventRecord(ev[5], s));
+        launch_update(c->geo, b, c->d_color, c->d_rho, c->d_area, c->d_rad, c->d_state, s);
+        RAD_CUDA(c, cudaEventRecord(ev[6], s));
+        launch_emitters(c->geo, b, c->d_rad, c->d_illum, c->d_area, c->cfg.tolerance, nullptr, c->d_state, s);
+        RAD_CUDA(c, cudaEventRecord(ev[7], s));
+        RAD_CUDA(c, cudaGetLastError());
+        RAD_CUDA(c, cudaEventSynchronize(ev[7]));
+        for (int k = 0; k < RAD_N_STAGES; k++) {
+            float ms = 0;
+            RAD_CUDA(c, cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+            stage_ms[k] += ms;
+            total_ms += ms;
+        }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    DevState after;
+    RAD_CUDA(c, cudaMemcpyAsync(&after, c->d_state, sizeof(after), cudaMemcpyDeviceToHost, s));
+    RAD_CUDA(c, cudaStreamSynchronize(s));
+    if (stats) {
+        stats->shots_done = after.shots_done - before.shots_done;
+        stats->stopped = after.stopped;
+        std::memcpy(stats->last_energy, after.last_energy, sizeof(float) * 3);
+        stats->residual = after.residual;
+        stats->hemicubes = after.hemicubes - before.hemicubes;
+        stats->device_ms = total_ms;
+    }
+    if (after.overflow) return fail(c, RAD_E_OVERFLOW, "triangle or bin capacity exceeded");
+    return RAD_OK;
+}
+
 const char* rad_strerror(int status) {
     switch (status) {
         case RAD_OK: return "ok";
