@@ -22,6 +22,7 @@ extern "C" {
 #define RAD_E_STATE (-4)    /* call out of order (e.g. no scene uploaded) */
 #define RAD_E_NOMEM (-5)    /* device allocation failed */
 #define RAD_E_TIMEOUT (-6)  /* a bounded device wait gave up */
+#define RAD_E_NOALLOC_LIMIT (-7) /* request larger than the allocation-free entry point's fixed scratch */
 
 typedef enum { RAD_MODE_REF = 0, RAD_MODE_PHYS = 1 } rad_mode;
 
@@ -128,6 +129,23 @@ int rad_profile_stages(rad_ctx* ctx, uint32_t n_shots, double* stage_ms, rad_sta
  * NULL arrays to get *n; then again with arrays of capacity >= *n patches. */
 int rad_scene_reference(double max_patch_area, uint32_t capacity, uint32_t* n, float* vertices,
                         int32_t* indices, float* color, float* radiosity, float* illumination);
+
+/* Allocation-free form-factor rows.  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory (their device memory belongs to another
+ * allocator's pool, or their loop must not allocate per call).  Inputs and outputs are
+ * the caller's DEVICE buffers: d_items holds `count` stacked 2W x 1.5W uint32 item
+ * buffers (0 = nothing, else patch index + 1; ids above n_patches are ignored) and
+ * d_ff_rows receives count x n_patches floats, the same values rad_reduce_item_buffers
+ * returns.  `stream` is a cudaStream_t (NULL = default stream); the call returns after
+ * the stream has finished the work.  No rad_ctx, no cudaMalloc/cudaFree: the only
+ * scratch is a fixed device array of RAD_NOALLOC_MAX_SUMS 64-bit sums (8 MiB) that every
+ * GPU loading the library holds until exit, so count * n_patches must not exceed
+ * RAD_NOALLOC_MAX_SUMS (else RAD_E_NOALLOC_LIMIT).  The first call on a device looks the
+ * array up (make it before any stream capture); calls that overlap on the GPU race on
+ * the shared array. */
+#define RAD_NOALLOC_MAX_SUMS (1u << 20)
+int rad_reduce_items_noalloc(const uint32_t* d_items, uint32_t count, uint32_t hemicube_side,
+                             uint32_t n_patches, float* d_ff_rows, void* stream);
 
 const char* rad_strerror(int status);
 const char* rad_last_error(const rad_ctx* ctx);

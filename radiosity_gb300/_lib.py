@@ -23,6 +23,8 @@ RAD_E_OVERFLOW = -3
 RAD_E_STATE = -4
 RAD_E_NOMEM = -5
 RAD_E_TIMEOUT = -6
+RAD_E_NOALLOC_LIMIT = -7
+NOALLOC_MAX_SUMS = 1 << 20
 MODE_REF, MODE_PHYS = 0, 1
 
 # Every symbol include/radiosity.h declares.
@@ -30,7 +32,7 @@ EXPORTS = [
     "rad_config_default", "rad_config_derived", "rad_create", "rad_destroy", "rad_upload_scene",
     "rad_set_state", "rad_download", "rad_ff_table", "rad_select_shooters", "rad_render_item_buffers",
     "rad_reduce_item_buffers", "rad_ff_rows", "rad_shoot", "rad_profile_stages", "rad_scene_reference",
-    "rad_strerror", "rad_last_error",
+    "rad_reduce_items_noalloc", "rad_strerror", "rad_last_error",
 ]
 STAGES = ["select", "camera", "setup", "bins", "raster", "update", "emitters"]
 STAGE_KERNELS = [1, 1, 1, 2, 1, 1, 1]
@@ -98,6 +100,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rad_shoot.argtypes = [vp, ctypes.c_uint32, P(RadStats)]
     L.rad_profile_stages.argtypes = [vp, ctypes.c_uint32, np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS"),
                                      P(RadStats)]
+    L.rad_reduce_items_noalloc.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp, vp]
     L.rad_scene_reference.argtypes = [ctypes.c_double, ctypes.c_uint32, P(ctypes.c_uint32), vp, vp, vp, vp, vp]
     L.rad_strerror.argtypes = [ctypes.c_int]
     L.rad_strerror.restype = ctypes.c_char_p

@@ -620,6 +620,7 @@ const char* rad_strerror(int status) {
         case RAD_E_STATE: return "call out of order";
         case RAD_E_NOMEM: return "device allocation failed";
         case RAD_E_TIMEOUT: return "bounded device wait gave up";
+        case RAD_E_NOALLOC_LIMIT: return "count * n_patches exceeds RAD_NOALLOC_MAX_SUMS (allocation-free scratch)";
         default: return "unknown status";
     }
 }
