@@ -50,6 +50,7 @@ def parse():
     p.add_argument("--seed", type=int, default=0)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-autotune", action="store_true", help="keep the default raster configuration")
     return p.parse_args()
 
 
@@ -230,12 +231,18 @@ def run_ours(args):
 
             dist.barrier()
 
+    tuning = None
+    if not args.no_autotune:  # picks the raster bin side and lane/warp split (state untouched)
+        t = solver.autotune(tune_k=False)
+        tuning = {"tile": t.tile, "small_tri_pixels": t.small_tri_pixels, "candidates": t.candidates,
+                  "us_per_hemicube": t.us_per_hemicube}
     # warm-up (graph capture happens on the first call)
     solver.shoot(args.warmup)
     # live per-stage timing (events between stages on the solver stream)
     solver.set_state(radiosity=sc["radiosity"], illumination=sc["illumination"])
     stage_ms, pst = solver.profile_stages(min(args.steps, 8))
     prof_batches = max(1, int(pst.shots_done))
+    counters = {k: v / max(1.0, pst.hemicubes) for k, v in solver.raster_counters().items()}
     # timed region: device-resident state, graph replays
     solver.set_state(radiosity=sc["radiosity"], illumination=sc["illumination"])
     solver.shoot(1)
@@ -288,7 +295,8 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded procedural room, 40 boxes, 4 emitters)",
         "config": config_block(args, sc, K, {"tile": int(solver.cfg.tile) or "auto",
-                                             "wall_s": wall, "residual_after": st.residual}),
+                                             "small_tri_pixels": int(solver.cfg.small_tri_pixels) or 64,
+                                             "autotune": tuning, "wall_s": wall, "residual_after": st.residual}),
         "e2e": {"value": e2e_hemi / e2e_s, "unit": "hemicubes/s",
                 "h2d_bytes_per_step": int(2 * 3 * 4 * n), "d2h_bytes_per_step": int(2 * 3 * 4 * n),
                 "steps": e2e_steps},
@@ -297,6 +305,7 @@ def run_ours(args):
                      "peak_kind": peak_kind, "traffic": ncu_traffic(K),
                      "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_ms": raster_ms},
         "stage_ms_per_step": {k: v / batches for k, v in stage_ms.items()},
+        "raster_counters_per_hemicube": counters,
         "gpu_launches": int(launches_per_step * st.shots_done),
         "clocks": ck,
     }

@@ -39,6 +39,8 @@ typedef struct rad_config {
     uint32_t tri_capacity;    /* triangle records per hemicube; 0 = 2*N + 4096 */
     uint32_t binref_capacity; /* bin references per hemicube; 0 = 4 * tri_capacity */
     int32_t device;           /* CUDA device ordinal */
+    uint32_t small_tri_pixels;/* triangles whose clamped bin area is at most this many pixels (and whose
+                                 extent is at most 64 px) are rasterised by one lane; 0 = 64 */
 } rad_config;
 
 typedef struct rad_stats {
@@ -123,6 +125,28 @@ int rad_shoot(rad_ctx* ctx, uint32_t n_shots, rad_stats* stats);
  * each stage's device milliseconds to stage_ms[RAD_N_STAGES] (caller zeroes it).
  * The state advances exactly as with rad_shoot.  stats may be NULL. */
 int rad_profile_stages(rad_ctx* ctx, uint32_t n_shots, double* stage_ms, rad_stats* stats);
+
+/* Result of rad_autotune. */
+typedef struct rad_tuning {
+    uint32_t tile;             /* chosen raster bin side */
+    uint32_t small_tri_pixels; /* chosen lane/warp split */
+    uint32_t hemicubes_count;  /* chosen K (unchanged unless RAD_TUNE_K) */
+    uint32_t candidates;       /* configurations timed */
+    double us_per_hemicube;    /* render + reduce time of the chosen configuration */
+} rad_tuning;
+
+#define RAD_TUNE_K 1u /* also choose K among 8..128 (changes the batching of the solve) */
+
+/* Times the hemicube render + reduce pipeline on the current top shooters for each
+ * candidate raster configuration (bin side 16/32/64 x lane/warp split 16..256 px,
+ * optionally K) and reconfigures the context with the fastest.  The radiosity state is
+ * not modified.  out may be NULL. */
+int rad_autotune(rad_ctx* ctx, uint32_t flags, rad_tuning* out);
+
+/* Raster counters of the last rad_profile_stages call (8 values): triangle-bin pairs,
+ * small triangles (one lane each), their bbox pixels, large triangles (one warp each),
+ * their 8x4 stamps, stamps visited, stamps wholly inside, large-triangle pixels written. */
+int rad_raster_counters(rad_ctx* ctx, uint64_t* out);
 
 /* Builds the reference scene (ModelContainer::load, source/ModelContainer.cpp:89-110,
  * PrimitiveModel ROOM/ROOMCLOSURE/CUBE/BLOCK subdivided to max_patch_area).  Call with

@@ -32,7 +32,7 @@ EXPORTS = [
     "rad_config_default", "rad_config_derived", "rad_create", "rad_destroy", "rad_upload_scene",
     "rad_set_state", "rad_download", "rad_ff_table", "rad_select_shooters", "rad_render_item_buffers",
     "rad_reduce_item_buffers", "rad_ff_rows", "rad_shoot", "rad_profile_stages", "rad_scene_reference",
-    "rad_reduce_items_noalloc", "rad_strerror", "rad_last_error",
+    "rad_reduce_items_noalloc", "rad_raster_counters", "rad_autotune", "rad_strerror", "rad_last_error",
 ]
 STAGES = ["select", "camera", "setup", "bins", "raster", "update", "emitters"]
 STAGE_KERNELS = [1, 1, 1, 2, 1, 1, 1]
@@ -51,6 +51,17 @@ class RadConfig(ctypes.Structure):
         ("tri_capacity", ctypes.c_uint32),
         ("binref_capacity", ctypes.c_uint32),
         ("device", ctypes.c_int32),
+        ("small_tri_pixels", ctypes.c_uint32),
+    ]
+
+
+class RadTuning(ctypes.Structure):
+    _fields_ = [
+        ("tile", ctypes.c_uint32),
+        ("small_tri_pixels", ctypes.c_uint32),
+        ("hemicubes_count", ctypes.c_uint32),
+        ("candidates", ctypes.c_uint32),
+        ("us_per_hemicube", ctypes.c_double),
     ]
 
 
@@ -100,6 +111,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rad_shoot.argtypes = [vp, ctypes.c_uint32, P(RadStats)]
     L.rad_profile_stages.argtypes = [vp, ctypes.c_uint32, np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS"),
                                      P(RadStats)]
+    L.rad_autotune.argtypes = [vp, ctypes.c_uint32, P(RadTuning)]
+    L.rad_raster_counters.argtypes = [vp, np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")]
     L.rad_reduce_items_noalloc.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp, vp]
     L.rad_scene_reference.argtypes = [ctypes.c_double, ctypes.c_uint32, P(ctypes.c_uint32), vp, vp, vp, vp, vp]
     L.rad_strerror.argtypes = [ctypes.c_int]
@@ -256,6 +269,23 @@ class Solver:
         st = RadStats()
         self._check(self.L.rad_profile_stages(self.h, n_shots, ms, ctypes.byref(st)), "rad_profile_stages")
         return dict(zip(STAGES, ms.tolist())), st
+
+    def autotune(self, tune_k: bool = False) -> RadTuning:
+        """rad_autotune: picks bin side and lane/warp split (and K when tune_k) by timing."""
+        t = RadTuning()
+        self._check(self.L.rad_autotune(self.h, 1 if tune_k else 0, ctypes.byref(t)), "rad_autotune")
+        self.cfg.tile = t.tile
+        self.cfg.small_tri_pixels = t.small_tri_pixels
+        self.cfg.hemicubes_count = t.hemicubes_count
+        return t
+
+    RASTER_COUNTERS = ["pairs", "small_tris", "small_px", "big_tris", "big_stamps", "stamps_visited",
+                       "stamps_inside", "big_px_written"]
+
+    def raster_counters(self) -> dict:
+        out = np.zeros(8, np.uint64)
+        self._check(self.L.rad_raster_counters(self.h, out), "rad_raster_counters")
+        return dict(zip(self.RASTER_COUNTERS, [int(x) for x in out]))
 
     def shoot(self, n_shots: int) -> RadStats:
         st = RadStats()

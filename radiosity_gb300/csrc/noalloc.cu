@@ -24,7 +24,7 @@
 
 #include <mutex>
 
-#include "../../include/radiosity.h"
+#include "radiosity.h"
 
 namespace {
 

@@ -9,13 +9,14 @@
 // the stop rule fired are no-ops and the result equals the reference's early exit.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
 
-#include "../../include/radiosity.h"
+#include "radiosity.h"
 #include "rad_internal.cuh"
 
 namespace rad {
@@ -93,6 +94,12 @@ static void free_batch(BatchBuf& bb) {
     dfree(bb.b.bin_list);
     dfree(bb.b.Fq);
     dfree(bb.b.items);
+    dfree(bb.b.sel_hist);
+    dfree(bb.b.sel_ctrl);
+    dfree(bb.b.sel_keys);
+    dfree(bb.b.sel_sure);
+    dfree(bb.b.sel_bnd);
+    dfree(bb.b.partials);
     bb.cap_k = 0;
     bb.has_items = false;
 }
@@ -132,6 +139,13 @@ static int alloc_batch(rad_ctx* c, BatchBuf& bb, uint32_t K, bool items) {
     RAD_CUDA(c, cudaMemsetAsync(b.Fq, 0, sizeof(unsigned long long) * (size_t)K * c->n, c->stream));
     RAD_CUDA(c, cudaMemsetAsync(b.valid, 0, sizeof(uint32_t) * K, c->stream));
     if (items) RAD_CUDA(c, cudaMalloc(&b.items, sizeof(uint32_t) * (size_t)K * c->geo.RES));
+    RAD_CUDA(c, cudaMalloc(&b.sel_hist, sizeof(uint32_t) * 2048));
+    RAD_CUDA(c, cudaMemsetAsync(b.sel_hist, 0, sizeof(uint32_t) * 2048, c->stream));
+    RAD_CUDA(c, cudaMalloc(&b.sel_ctrl, sizeof(uint32_t) * 8));
+    RAD_CUDA(c, cudaMalloc(&b.sel_keys, sizeof(uint32_t) * c->n));
+    RAD_CUDA(c, cudaMalloc(&b.sel_sure, sizeof(unsigned long long) * K));
+    RAD_CUDA(c, cudaMalloc(&b.sel_bnd, sizeof(unsigned long long) * c->n));
+    RAD_CUDA(c, cudaMalloc(&b.partials, sizeof(double) * kUpdateBlocks));
     b.bins = c->d_bins;
     bb.cap_k = K;
     bb.has_items = items;
@@ -156,6 +170,7 @@ static void setup_geo(rad_ctx* c, std::vector<BinInfo>& bins) {
     uint32_t tile = c->cfg.tile;
     if (tile == 0) tile = W >= 512 ? 64 : (W >= 64 ? 32 : 16);
     g.tile = tile;
+    g.small_max = c->cfg.small_tri_pixels ? c->cfg.small_tri_pixels : 64;
     const int w = (int)W, h = (int)W;
     uint32_t base = 0;
     bins.clear();
@@ -221,6 +236,7 @@ static int check_cfg(const rad_config* cfg) {
     if (cfg->tile != 0 && cfg->tile != 16 && cfg->tile != 32 && cfg->tile != 64) return RAD_E_INVALID;
     if (cfg->mode > 1) return RAD_E_INVALID;
     if (cfg->ocl_workitems_x == 0) return RAD_E_INVALID;
+    if (cfg->small_tri_pixels > 4096) return RAD_E_INVALID;
     return RAD_OK;
 }
 
@@ -314,7 +330,6 @@ int rad_create(const rad_config* cfg, rad_ctx** out) {
     if (check_cfg(cfg) != RAD_OK) return RAD_E_INVALID;
     rad_ctx* c = new rad_ctx();
     c->cfg = *cfg;
-    int rc = RAD_OK;
     auto bail = [&](int code) {
         rad_destroy(c);
         return code;
@@ -335,7 +350,6 @@ int rad_create(const rad_config* cfg, rad_ctx** out) {
     cudaMemsetAsync(c->d_aux, 0, sizeof(DevState), c->stream);
     launch_fftab(c->geo.W, c->d_fftab, c->stream);
     if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(c->stream) != cudaSuccess) return bail(RAD_E_CUDA);
-    (void)rc;
     *out = c;
     return RAD_OK;
 }
@@ -568,6 +582,7 @@ int rad_profile_stages(rad_ctx* c, uint32_t n_shots, double* stage_ms, rad_stats
     RAD_CUDA(c, cudaMemcpyAsync(&before, c->d_state, sizeof(before), cudaMemcpyDeviceToHost, s));
     RAD_CUDA(c, cudaStreamSynchronize(s));
     float total_ms = 0;
+    RAD_CUDA(c, cudaMemsetAsync(c->d_state->raster_counters, 0, sizeof(c->d_state->raster_counters), s));
     for (uint32_t shot = 0; shot < n_shots; shot++) {
         RAD_CUDA(c, cudaMemsetAsync(&c->d_state->tri_count, 0, sizeof(uint32_t), s));
         RAD_CUDA(c, cudaMemsetAsync(b.bin_count, 0, sizeof(uint32_t) * (size_t)b.K * c->geo.nb, s));
@@ -580,7 +595,7 @@ int rad_profile_stages(rad_ctx* c, uint32_t n_shots, double* stage_ms, rad_stats
         RAD_CUDA(c, cudaEventRecord(ev[3], s));
         launch_bins(c->geo, b, c->d_state, s);
         RAD_CUDA(c, cudaEventRecord(ev[4], s));
-        launch_raster(c->geo, b, c->d_fftab, c->d_state, false, true, s);
+        launch_raster(c->geo, b, c->d_fftab, c->d_state, false, true, s, true);
         RAD_CUDA(c, cudaEventRecord(ev[5], s));
         launch_update(c->geo, b, c->d_color, c->d_rho, c->d_area, c->d_rad, c->d_state, s);
         RAD_CUDA(c, cudaEventRecord(ev[6], s));
@@ -608,6 +623,133 @@ int rad_profile_stages(rad_ctx* c, uint32_t n_shots, double* stage_ms, rad_stats
         stats->device_ms = total_ms;
     }
     if (after.overflow) return fail(c, RAD_E_OVERFLOW, "triangle or bin capacity exceeded");
+    return RAD_OK;
+}
+
+// Re-derives the raster geometry for a new bin side / split / K and reallocates the
+// batch buffers (the scene and the radiosity state stay on the device).
+static int reconfigure(rad_ctx* c, uint32_t tile, uint32_t small, uint32_t K) {
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    drop_graph(c);
+    free_batch(c->shoot);
+    free_batch(c->aux);
+    c->cfg.tile = tile;
+    c->cfg.small_tri_pixels = small;
+    c->cfg.hemicubes_count = K;
+    const uint32_t n = c->geo.n;
+    std::vector<BinInfo> bins;
+    setup_geo(c, bins);
+    c->geo.n = n;
+    dfree(c->d_bins);
+    RAD_CUDA(c, cudaMalloc(&c->d_bins, sizeof(BinInfo) * bins.size()));
+    RAD_CUDA(c, cudaMemcpy(c->d_bins, bins.data(), sizeof(BinInfo) * bins.size(), cudaMemcpyHostToDevice));
+    return alloc_batch(c, c->shoot, K, false);
+}
+
+// Device time of render + reduce of `count` shooters with the aux batch (best of reps).
+static int time_pipeline(rad_ctx* c, const std::vector<uint32_t>& sh, int reps, float* best_ms) {
+    const uint32_t count = (uint32_t)sh.size();
+    int rc = alloc_batch(c, c->aux, count, false);
+    if (rc) return rc;
+    Batch& b = c->aux.b;
+    b.K = count;
+    cudaStream_t s = c->stream;
+    std::vector<uint32_t> ones(count, 1u);
+    RAD_CUDA(c, cudaMemcpyAsync(b.shooters, sh.data(), sizeof(uint32_t) * count, cudaMemcpyHostToDevice, s));
+    RAD_CUDA(c, cudaMemcpyAsync(b.valid, ones.data(), sizeof(uint32_t) * count, cudaMemcpyHostToDevice, s));
+    *best_ms = 1e30f;
+    for (int r = 0; r < reps + 1; r++) {
+        RAD_CUDA(c, cudaMemsetAsync(c->d_aux, 0, sizeof(DevState), s));
+        RAD_CUDA(c, cudaMemsetAsync(b.bin_count, 0, sizeof(uint32_t) * (size_t)count * c->geo.nb, s));
+        RAD_CUDA(c, cudaEventRecord(c->ev0, s));
+        launch_camera(c->geo, b, c->d_verts, c->d_rad, c->d_aux, s);
+        launch_setup(c->geo, b, c->d_verts, c->d_aux, s);
+        launch_bins(c->geo, b, c->d_aux, s);
+        launch_raster(c->geo, b, c->d_fftab, c->d_aux, false, true, s);
+        RAD_CUDA(c, cudaEventRecord(c->ev1, s));
+        RAD_CUDA(c, cudaMemsetAsync(b.Fq, 0, sizeof(unsigned long long) * (size_t)count * c->n, s));
+        RAD_CUDA(c, cudaGetLastError());
+        RAD_CUDA(c, cudaEventSynchronize(c->ev1));
+        float ms = 0;
+        RAD_CUDA(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+        if (r > 0 && ms < *best_ms) *best_ms = ms;  // first pass warms up
+    }
+    DevState st;
+    RAD_CUDA(c, cudaMemcpy(&st, c->d_aux, sizeof(st), cudaMemcpyDeviceToHost));
+    if (st.overflow) *best_ms = 1e30f;
+    return RAD_OK;
+}
+
+int rad_autotune(rad_ctx* c, uint32_t flags, rad_tuning* out) {
+    if (!c) return RAD_E_INVALID;
+    if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
+    // sample shooters: the current top K (or an even spread when nothing has energy)
+    const uint32_t K0 = c->cfg.hemicubes_count;
+    std::vector<uint32_t> ids(K0);
+    std::vector<uint8_t> valid(K0);
+    int rc = rad_select_shooters(c, ids.data(), valid.data());
+    if (rc) return rc;
+    std::vector<uint32_t> sh;
+    for (uint32_t k = 0; k < K0; k++)
+        if (valid[k]) sh.push_back(ids[k]);
+    const uint32_t want = std::max<uint32_t>(8, std::min<uint32_t>(K0, 64));
+    for (uint32_t i = 0; sh.size() < want && i < want; i++) sh.push_back((uint32_t)(((uint64_t)i * 2654435761u) % c->n));
+    const uint32_t tiles[3] = {16, 32, 64};
+    const uint32_t smalls[5] = {16, 32, 64, 128, 256};
+    uint32_t best_t = 0, best_s = 0, cand = 0;
+    float best = 1e30f;
+    for (uint32_t t : tiles) {
+        if (t > c->geo.W) continue;
+        for (uint32_t sm : smalls) {
+            if ((rc = reconfigure(c, t, sm, K0))) return rc;
+            float ms;
+            if ((rc = time_pipeline(c, sh, 2, &ms))) return rc;
+            cand++;
+            if (ms < best) {
+                best = ms;
+                best_t = t;
+                best_s = sm;
+            }
+        }
+    }
+    if (best_t == 0) return fail(c, RAD_E_OVERFLOW, "no raster configuration fit the capacities");
+    uint32_t best_k = K0;
+    if (flags & RAD_TUNE_K) {
+        // throughput of the whole batch at K; the smallest K within 10% of the best rate wins
+        const uint32_t ks[5] = {8, 16, 32, 64, 128};
+        double rate[5] = {0, 0, 0, 0, 0}, top = 0;
+        for (int i = 0; i < 5; i++) {
+            if ((rc = reconfigure(c, best_t, best_s, ks[i]))) return rc;
+            std::vector<uint32_t> shk;
+            for (uint32_t k = 0; k < ks[i]; k++) shk.push_back(sh[k % sh.size()]);
+            float ms;
+            if ((rc = time_pipeline(c, shk, 2, &ms))) return rc;
+            rate[i] = ks[i] / (double)ms;
+            top = std::max(top, rate[i]);
+            cand++;
+        }
+        for (int i = 0; i < 5; i++)
+            if (rate[i] >= 0.9 * top) {
+                best_k = ks[i];
+                break;
+            }
+    }
+    if ((rc = reconfigure(c, best_t, best_s, best_k))) return rc;
+    if (out) {
+        out->tile = best_t;
+        out->small_tri_pixels = best_s;
+        out->hemicubes_count = best_k;
+        out->candidates = cand;
+        out->us_per_hemicube = 1000.0 * best / (double)sh.size();
+    }
+    return RAD_OK;
+}
+
+int rad_raster_counters(rad_ctx* c, uint64_t* out) {
+    if (!c || !out) return RAD_E_INVALID;
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    RAD_CUDA(c, cudaMemcpy(out, c->d_state->raster_counters, sizeof(c->d_state->raster_counters),
+                           cudaMemcpyDeviceToHost));
     return RAD_OK;
 }
 

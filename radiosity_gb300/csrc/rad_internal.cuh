@@ -50,6 +50,8 @@ struct Geo {
     uint32_t nb;               // bins per hemicube
     uint32_t tile;             // bin side
     uint32_t mode;             // rad_mode
+    uint32_t small_max;        // lane-mode threshold (clamped bbox pixels)
+    uint32_t pad0[3];
     FaceInfo face[5];
     float proj[16];            // Perspective(90,1,0.01,1000), column-major
 };
@@ -66,6 +68,9 @@ struct DevState {
     double hemicubes;
     uint32_t timeouts;
     uint32_t pad[3];
+    // raster counters (filled when counting is on): tri-bin pairs, small tris, small bbox px,
+    // big tris, big stamps in bbox, stamps visited, stamps fully inside, big pixels plotted
+    unsigned long long raster_counters[8];
 };
 
 // Device pointers of one batch of K hemicubes.
@@ -87,7 +92,15 @@ struct Batch {
     unsigned long long* Fq;      // K*N exact sums (scale 2^61)
     uint32_t* items;             // K*RES or null
     const BinInfo* bins;         // nb
+    // PHYS selection scratch
+    uint32_t* sel_hist;          // 2048 (cleared by the pick kernel after use)
+    uint32_t* sel_ctrl;          // 8
+    uint32_t* sel_keys;          // N
+    unsigned long long* sel_sure;  // K
+    unsigned long long* sel_bnd;   // N
+    double* partials;            // kUpdateBlocks FP64 residual partials
 };
+constexpr int kUpdateBlocks = 152 * 8;
 
 // Launchers (raster.cu / shoot.cu).  All run on `s`.
 void launch_camera(const Geo& g, const Batch& b, const float* verts, const float4* rad, DevState* st,
@@ -95,7 +108,7 @@ void launch_camera(const Geo& g, const Batch& b, const float* verts, const float
 void launch_setup(const Geo& g, const Batch& b, const float* verts, DevState* st, cudaStream_t s);
 void launch_bins(const Geo& g, const Batch& b, DevState* st, cudaStream_t s);
 void launch_raster(const Geo& g, const Batch& b, const float* fftab, DevState* st, bool write_items,
-                   bool fused_reduce, cudaStream_t s);
+                   bool fused_reduce, cudaStream_t s, bool count = false);
 void launch_reduce_items(const Geo& g, const Batch& b, const float* fftab, uint32_t count, cudaStream_t s);
 void launch_fq_to_float(const Geo& g, const Batch& b, uint32_t count, float* out, cudaStream_t s);
 void launch_select(const Geo& g, const Batch& b, const float4* rad, const float* area, DevState* st,

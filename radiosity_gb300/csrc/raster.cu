@@ -188,8 +188,9 @@ struct SV {
     float D;
 };
 
-// Triangle record for (a, b, c); false when culled (area <= 0) or outside the scissor.
-__device__ __forceinline__ bool make_tri(SV a, SV b, SV c, uint32_t id, const FaceInfo& F, TriRec& t) {
+// Cull test of (a, b, c): CCW with positive area and a non-empty pixel bbox inside
+// the scissor; the bbox is returned in px (x0, x1, y0, y1).
+__device__ __forceinline__ bool tri_bbox(SV a, SV b, SV c, const FaceInfo& F, int* px) {
     long long area2 = ((long long)b.X - a.X) * ((long long)c.Y - a.Y) - ((long long)c.X - a.X) * ((long long)b.Y - a.Y);
     if (area2 <= 0) return false;
     int32_t xmin = min(a.X, min(b.X, c.X)), xmax = max(a.X, max(b.X, c.X));
@@ -202,6 +203,16 @@ __device__ __forceinline__ bool make_tri(SV a, SV b, SV c, uint32_t id, const Fa
     if (px1 > sc[0] + sc[2] - 1) px1 = sc[0] + sc[2] - 1;
     if (py1 > sc[1] + sc[3] - 1) py1 = sc[1] + sc[3] - 1;
     if (px0 > px1 || py0 > py1) return false;
+    px[0] = (int)px0; px[1] = (int)px1; px[2] = (int)py0; px[3] = (int)py1;
+    return true;
+}
+
+// Writes the record of a triangle that passed tri_bbox: vertices, depth plane, id, bbox.
+__device__ __forceinline__ void tri_write(SV a, SV b, SV c, uint32_t id, uint32_t hf, const FaceInfo& F, const int* px,
+                                          TriRec* out) {
+    const long long area2 =
+        ((long long)b.X - a.X) * ((long long)c.Y - a.Y) - ((long long)c.X - a.X) * ((long long)b.Y - a.Y);
+    const int* sc = F.sc;
     float fa = (float)area2;
     float e1x = (float)((long long)b.X - a.X), e1y = (float)((long long)b.Y - a.Y);
     float e2x = (float)((long long)c.X - a.X), e2y = (float)((long long)c.Y - a.Y);
@@ -209,41 +220,76 @@ __device__ __forceinline__ bool make_tri(SV a, SV b, SV c, uint32_t id, const Fa
     float gx = (d1 * e2y - d2 * e1y) / fa;
     float gy = (d2 * e1x - d1 * e2x) / fa;
     float ox = (float)((long long)sc[0] * 256 + 128 - a.X), oy = (float)((long long)sc[1] * 256 + 128 - a.Y);
-    t.X0 = a.X; t.Y0 = a.Y; t.X1 = b.X; t.Y1 = b.Y; t.X2 = c.X; t.Y2 = c.Y;
-    t.c0 = (a.D + gx * ox) + gy * oy;
-    t.ax = gx * 256.0f;
-    t.ay = gy * 256.0f;
-    t.id = id;
-    t.px0 = (int16_t)px0; t.px1 = (int16_t)px1; t.py0 = (int16_t)py0; t.py1 = (int16_t)py1;
-    return true;
+    int4* o = reinterpret_cast<int4*>(out);
+    o[0] = make_int4(a.X, a.Y, b.X, b.Y);
+    o[1] = make_int4(c.X, c.Y, __float_as_int((a.D + gx * ox) + gy * oy), __float_as_int(gx * 256.0f));
+    o[2] = make_int4(__float_as_int(gy * 256.0f), (int)id, (int)((uint32_t)(uint16_t)px[0] | ((uint32_t)px[1] << 16)),
+                     (int)((uint32_t)(uint16_t)px[2] | ((uint32_t)px[3] << 16)));
+    o[3] = make_int4((int)hf, 0, 0, 0);
 }
 
 __device__ __forceinline__ void count_bins(const Geo& g, const Batch& b, uint32_t hi, const FaceInfo& F,
-                                           const TriRec& t) {
+                                           const int* px) {
     const int tile = (int)g.tile;
-    int c0 = (t.px0 - F.sc[0]) / tile, c1 = (t.px1 - F.sc[0]) / tile;
-    int r0 = (t.py0 - F.sc[1]) / tile, r1 = (t.py1 - F.sc[1]) / tile;
+    int c0 = (px[0] - F.sc[0]) / tile, c1 = (px[1] - F.sc[0]) / tile;
+    int r0 = (px[2] - F.sc[1]) / tile, r1 = (px[3] - F.sc[1]) / tile;
     uint32_t* cnt = b.bin_count + (size_t)hi * g.nb + F.bin_base;
     for (int r = r0; r <= r1; r++)
         for (int c = c0; c <= c1; c++) atomicAdd(&cnt[r * F.bins_x + c], 1u);
 }
 
-__global__ void __launch_bounds__(128) k_setup(Geo g, Batch b, const float* __restrict__ verts, DevState* st) {
+// Snap one clip-space vertex to 24.8 fixed-point window coordinates; false when w <= 0.
+__device__ __forceinline__ bool snap_vertex(float4 c, float hw, float hh, float vx, float vy, SV& o) {
+    if (!(c.w > 0)) return false;
+    const float xd = c.x / c.w, yd = c.y / c.w;
+    const float xw = (xd + 1.0f) * hw + vx, yw = (yd + 1.0f) * hh + vy;
+    o.X = (int32_t)__float2ll_rn(xw * 256.0f);
+    o.Y = (int32_t)__float2ll_rn(yw * 256.0f);
+    o.D = 1.0f / c.w;
+    return true;
+}
+
+// Fan triangles of a clipped polygon into slots base .. base+pn-3 (culled ones marked dead).
+__device__ __noinline__ void emit_polygon(const Geo& g, const Batch& b, const float4* poly, int pn, uint32_t base,
+                                          uint32_t p, uint32_t hi, int f, float hw, float hh, float vx, float vy,
+                                          DevState* st) {
+    const FaceInfo& F = g.face[f];
+    SV sv[12];
+    bool good = true;
+    for (int k = 0; k < pn; k++) good = good && snap_vertex(poly[k], hw, hh, vx, vy, sv[k]);
+    for (int j = 0; j + 2 < pn; j++) {
+        const uint32_t slot = base + (uint32_t)j;
+        if (slot >= b.tri_cap) {
+            atomicOr(&st->overflow, 1u);
+            return;
+        }
+        int px[4];
+        if (good && tri_bbox(sv[0], sv[j + 1], sv[j + 2], F, px)) {
+            tri_write(sv[0], sv[j + 1], sv[j + 2], p, hi * 5 + (uint32_t)f, F, px, &b.tris[slot]);
+            count_bins(g, b, hi, F, px);
+        } else {
+            b.tris[slot].id = kDeadTri;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128, 5) k_setup(Geo g, Batch b, const float* __restrict__ verts, DevState* st) {
     if (st->stopped) return;
     const uint32_t hi = blockIdx.y;
     if (!b.valid[hi]) return;
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     bool active = p < g.n;
-    const float* fr = b.frame + (size_t)hi * 8;
-    const float cx = fr[0], cy = fr[1], cz = fr[2], nx = fr[3], ny = fr[4], nz = fr[5];
+    __shared__ float s_mvp[5 * 16];
+    __shared__ float s_fr[8];
+    for (int i = threadIdx.x; i < 5 * 16; i += blockDim.x) s_mvp[i] = b.mvp[(size_t)hi * 80 + i];
+    if (threadIdx.x < 8) s_fr[threadIdx.x] = b.frame[(size_t)hi * 8 + threadIdx.x];
+    __syncthreads();
+    const float cx = s_fr[0], cy = s_fr[1], cz = s_fr[2], nx = s_fr[3], ny = s_fr[4], nz = s_fr[5];
     float4 cv[4];
-    float q[12];
+    const float4* src = reinterpret_cast<const float4*>(verts + 12 * (size_t)(active ? p : 0));
     if (active) {
-        const float4* src = reinterpret_cast<const float4*>(verts + 12 * (size_t)p);
-        float4 a = __ldg(src), bq = __ldg(src + 1), c = __ldg(src + 2);
-        q[0] = a.x; q[1] = a.y; q[2] = a.z; q[3] = a.w;
-        q[4] = bq.x; q[5] = bq.y; q[6] = bq.z; q[7] = bq.w;
-        q[8] = c.x; q[9] = c.y; q[10] = c.z; q[11] = c.w;
+        const float4 a = __ldg(src), bq = __ldg(src + 1), c = __ldg(src + 2);
+        const float q[12] = {a.x, a.y, a.z, a.w, bq.x, bq.y, bq.z, bq.w, c.x, c.y, c.z, c.w};
         bool behind = true;
 #pragma unroll
         for (int k = 0; k < 4; k++) {
@@ -256,11 +302,10 @@ __global__ void __launch_bounds__(128) k_setup(Geo g, Batch b, const float* __re
         const FaceInfo& F = g.face[f];
         bool fa = active;
         if (fa) {
-            const float* m = b.mvp + ((size_t)hi * 5 + f) * 16;
-            float mm[16];
-#pragma unroll
-            for (int i = 0; i < 16; i++) mm[i] = __ldg(m + i);
+            const float* mm = s_mvp + f * 16;
             uint32_t out_any = 0x3F, in_half = 0;
+            const float4 qa = __ldg(src), qb = __ldg(src + 1), qc = __ldg(src + 2);
+            const float q[12] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w};
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 float x = q[3 * k], y = q[3 * k + 1], z = q[3 * k + 2];
@@ -290,48 +335,38 @@ __global__ void __launch_bounds__(128) k_setup(Geo g, Batch b, const float* __re
         }
         const float hw = 0.5f * (float)F.vp[2], hh = 0.5f * (float)F.vp[3];
         const float vx = (float)F.vp[0], vy = (float)F.vp[1];
+#pragma unroll
         for (int t = 0; t < 2; t++) {
+            const float4 va = cv[0], vb = cv[1 + t], vc = cv[2 + t];
+            const bool clip = fa && (needs_clip(va) || needs_clip(vb) || needs_clip(vc));
+            const bool fast = fa && !clip;
+            SV s0, s1, s2;
+            int px[4];
+            bool ok = false;
+            if (fast) {
+                const bool good = snap_vertex(va, hw, hh, vx, vy, s0) & snap_vertex(vb, hw, hh, vx, vy, s1) &
+                                  snap_vertex(vc, hw, hh, vx, vy, s2);
+                ok = good && tri_bbox(s0, s1, s2, F, px);
+            }
             float4 poly[12];
             int pn = 0;
-            if (fa) {
-                poly[0] = cv[0];
-                poly[1] = cv[t == 0 ? 1 : 2];
-                poly[2] = cv[t == 0 ? 2 : 3];
-                pn = 3;
-                if (needs_clip(poly[0]) || needs_clip(poly[1]) || needs_clip(poly[2])) pn = clip_polygon(poly, 3);
+            if (clip) {
+                poly[0] = va;
+                poly[1] = vb;
+                poly[2] = vc;
+                pn = clip_polygon(poly, 3);
             }
-            SV sv[12];
-            if (pn >= 3) {
-                for (int k = 0; k < pn; k++) {
-                    float4 c = poly[k];
-                    if (!(c.w > 0)) {
-                        pn = 0;
-                        break;
-                    }
-                    float xd = c.x / c.w, yd = c.y / c.w;
-                    float xw = (xd + 1.0f) * hw + vx, yw = (yd + 1.0f) * hh + vy;
-                    sv[k].X = (int32_t)__float2ll_rn(xw * 256.0f);
-                    sv[k].Y = (int32_t)__float2ll_rn(yw * 256.0f);
-                    sv[k].D = 1.0f / c.w;
-                }
-            }
-            uint32_t ncand = pn >= 3 ? (uint32_t)(pn - 2) : 0u;
-            uint32_t base = warp_alloc(&st->tri_count, ncand);
-            for (uint32_t j = 0; j < ncand; j++) {
-                uint32_t slot = base + j;
-                if (slot >= b.tri_cap) {
+            const uint32_t ncand = fast ? (ok ? 1u : 0u) : (pn >= 3 ? (uint32_t)(pn - 2) : 0u);
+            const uint32_t base = warp_alloc(&st->tri_count, ncand);
+            if (fast && ok) {
+                if (base >= b.tri_cap) {
                     atomicOr(&st->overflow, 1u);
-                    break;
-                }
-                TriRec rec;
-                bool ok = make_tri(sv[0], sv[j + 1], sv[j + 2], p, F, rec);
-                if (ok) {
-                    rec.hf = hi * 5 + (uint32_t)f;
-                    b.tris[slot] = rec;
-                    count_bins(g, b, hi, F, rec);
                 } else {
-                    b.tris[slot].id = kDeadTri;
+                    tri_write(s0, s1, s2, p, hi * 5 + (uint32_t)f, F, px, &b.tris[base]);
+                    count_bins(g, b, hi, F, px);
                 }
+            } else if (ncand) {
+                emit_polygon(g, b, poly, pn, base, p, hi, f, hw, hh, vx, vy, st);
             }
         }
     }
@@ -418,18 +453,153 @@ __device__ __forceinline__ unsigned long long group_sum(uint32_t key, unsigned l
     return (unsigned long long)sa + ((unsigned long long)sb << 21) + ((unsigned long long)sc << 42);
 }
 
+constexpr int32_t kSmallExtent = 16384;  // 64 px in 24.8 fixed point: edge values fit int32
+constexpr int kChunk = 256;          // triangle records staged per CTA round
+constexpr int kHashSlots = 1024;     // per-bin id -> sum table of the reduction phase
+constexpr uint32_t kHashEmpty = 0xFFFFFFFFu;
+constexpr int kRegionBytes = 12 * kHashSlots;  // >= kChunk * sizeof(RTri) (10 KB)
+
+// The parts of a triangle record the per-pixel loops need (40 bytes in shared memory).
+struct RTri {
+    int32_t X[3], Y[3];
+    float c0, ax, ay;
+    uint32_t id;
+};
+
+__device__ __forceinline__ bool inside_edge(long long e, bool tl) { return e > 0 || (e == 0 && tl); }
+__device__ __forceinline__ bool inside_edge32(int32_t e, bool tl) { return e > 0 || (e == 0 && tl); }
+
+// One lane rasterises a small triangle over its clamped bbox [x0,x1]x[y0,y1] with
+// 32-bit incremental edge functions (exact: |E| < 2^30 for extents <= 64 px).
 template <int TILE>
-__global__ void __launch_bounds__(256) k_raster(Geo g, Batch b, const float* __restrict__ fftab, DevState* st,
-                                                int write_items, int fused) {
+__device__ __forceinline__ void raster_small(const RTri& t, int x0, int x1, int y0, int y1, const BinInfo& bi, int sx,
+                                             int sy, unsigned long long* key) {
+    int32_t er[3], stx[3], sty[3];
+    bool tl[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int j = k == 2 ? 0 : k + 1;
+        const int32_t dx = t.X[j] - t.X[k], dy = t.Y[j] - t.Y[k];
+        er[k] = dx * (y0 * 256 + 128 - t.Y[k]) - dy * (x0 * 256 + 128 - t.X[k]);
+        stx[k] = -dy * 256;
+        sty[k] = dx * 256;
+        tl[k] = (t.Y[j] < t.Y[k]) || (t.Y[j] == t.Y[k] && t.X[j] < t.X[k]);
+    }
+    for (int py = y0; py <= y1; py++) {
+        int32_t e0 = er[0], e1 = er[1], e2 = er[2];
+        const float w = (float)(py - sy);
+        for (int px = x0; px <= x1; px++) {
+            if (inside_edge32(e0, tl[0]) && inside_edge32(e1, tl[1]) && inside_edge32(e2, tl[2])) {
+                const float u = (float)(px - sx);
+                const float D = (t.c0 + t.ax * u) + t.ay * w;
+                const unsigned long long k = ((unsigned long long)depth_ordinal(D) << 32) | t.id;
+                atomicMin(&key[(py - bi.y0) * TILE + (px - bi.x0)], k);
+            }
+            e0 += stx[0];
+            e1 += stx[1];
+            e2 += stx[2];
+        }
+        er[0] += sty[0];
+        er[1] += sty[1];
+        er[2] += sty[2];
+    }
+}
+
+// One warp rasterises a large triangle in 8x4 stamps.  The 32 lanes first
+// classify 32 stamps at a time against the three edges (wholly outside one edge:
+// skipped; wholly inside all edges: no per-pixel edge test), then the warp walks
+// only the surviving stamps, one pixel per lane.  Edge values are exact int64.
+template <int TILE>
+__device__ __forceinline__ void raster_big(const RTri& t, int x0, int x1, int y0, int y1, const BinInfo& bi, int sx,
+                                           int sy, unsigned long long* key, int lane, uint32_t* cnt) {
+    long long eo[3], stx[3], sty[3], off[3];
+    bool tl[3];
+    const int lx = lane & 7, ly = lane >> 3;
+    long long mx[3], mn[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int j = k == 2 ? 0 : k + 1;
+        const long long dx = (long long)t.X[j] - t.X[k], dy = (long long)t.Y[j] - t.Y[k];
+        eo[k] = dx * ((long long)y0 * 256 + 128 - t.Y[k]) - dy * ((long long)x0 * 256 + 128 - t.X[k]);
+        stx[k] = -dy * 256;
+        sty[k] = dx * 256;
+        off[k] = stx[k] * lx + sty[k] * ly;
+        mx[k] = (stx[k] > 0 ? stx[k] * 7 : 0) + (sty[k] > 0 ? sty[k] * 3 : 0);
+        mn[k] = (stx[k] < 0 ? stx[k] * 7 : 0) + (sty[k] < 0 ? sty[k] * 3 : 0);
+        tl[k] = (t.Y[j] < t.Y[k]) || (t.Y[j] == t.Y[k] && t.X[j] < t.X[k]);
+    }
+    const int nsx = (x1 - x0 + 8) >> 3, nsy = (y1 - y0 + 4) >> 2, nst = nsx * nsy;
+    uint32_t visited = 0, accepted = 0, plotted = 0;
+    for (int base = 0; base < nst; base += 32) {
+        const int s = base + lane;
+        long long es[3] = {0, 0, 0};
+        bool live = false, acc = false;
+        int mcx = 0, mcy = 0;
+        if (s < nst) {
+            mcy = s / nsx;
+            mcx = (s - mcy * nsx) * 8;
+            mcy *= 4;
+            const long long cx = mcx, cy = mcy;
+            live = true;
+            acc = true;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                es[k] = eo[k] + stx[k] * cx + sty[k] * cy;
+                if (es[k] + mx[k] < 0) live = false;
+                if (!(es[k] + mn[k] > 0)) acc = false;
+            }
+        }
+        const unsigned lm = __ballot_sync(0xffffffffu, live), am = __ballot_sync(0xffffffffu, live && acc);
+        visited += __popc(lm);
+        accepted += __popc(am);
+        unsigned todo = lm;
+        while (todo) {
+            const int j = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int px = x0 + __shfl_sync(0xffffffffu, mcx, j) + lx, py = y0 + __shfl_sync(0xffffffffu, mcy, j) + ly;
+            const long long e0 = __shfl_sync(0xffffffffu, es[0], j), e1 = __shfl_sync(0xffffffffu, es[1], j),
+                            e2 = __shfl_sync(0xffffffffu, es[2], j);
+            bool in = px <= x1 && py <= y1;
+            if (in && !((am >> j) & 1u))
+                in = inside_edge(e0 + off[0], tl[0]) && inside_edge(e1 + off[1], tl[1]) &&
+                     inside_edge(e2 + off[2], tl[2]);
+            if (in) {
+                const float u = (float)(px - sx), w = (float)(py - sy);
+                const float D = (t.c0 + t.ax * u) + t.ay * w;
+                const unsigned long long k = ((unsigned long long)depth_ordinal(D) << 32) | t.id;
+                atomicMin(&key[(py - bi.y0) * TILE + (px - bi.x0)], k);
+                plotted++;
+            }
+        }
+    }
+    if (cnt && lane == 0) {
+        atomicAdd(&cnt[4], (uint32_t)nst);
+        atomicAdd(&cnt[5], visited);
+        atomicAdd(&cnt[6], accepted);
+    }
+    if (cnt) atomicAdd(&cnt[7], plotted);
+}
+
+template <int TILE>
+__global__ void __launch_bounds__(256, 3) k_raster(Geo g, Batch b, const float* __restrict__ fftab, DevState* st,
+                                                   int write_items, int fused, int count) {
     if (st->stopped) return;
     const uint32_t gb = blockIdx.x;
     const uint32_t hi = gb / g.nb, bin = gb % g.nb;
     const BinInfo bi = b.bins[bin];
     const bool valid = b.valid[hi] != 0;
     __shared__ unsigned long long key[TILE * TILE];
+    // one region, two uses: big-triangle staging during the raster phase, then the
+    // per-bin id -> exact-sum hash table of the reduction phase
+    __shared__ __align__(16) unsigned char s_region[kRegionBytes];
+    RTri* s_big = reinterpret_cast<RTri*>(s_region);
+    __shared__ int s_nbig;
+    __shared__ uint32_t s_cnt[8];
+    uint32_t* ctr = count ? s_cnt : nullptr;
+    if (threadIdx.x < 8) s_cnt[threadIdx.x] = 0;
     for (int j = threadIdx.x; j < TILE * TILE; j += blockDim.x) key[j] = ~0ull;
-    __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    __syncthreads();
     if (valid) {
         const FaceInfo& F = g.face[bi.face];
         const int sx = F.sc[0], sy = F.sc[1];
@@ -437,38 +607,71 @@ __global__ void __launch_bounds__(256) k_raster(Geo g, Batch b, const float* __r
         if (off >= b.list_cap) cnt = 0;
         else if (off + cnt > b.list_cap) cnt = b.list_cap - off;
         const int bx1 = bi.x0 + bi.w - 1, by1 = bi.y0 + bi.h - 1;
-        for (uint32_t i = warp; i < cnt; i += nwarp) {
-            const TriRec t = b.tris[b.bin_list[off + i]];
-            const int x0 = max((int)t.px0, (int)bi.x0), x1 = min((int)t.px1, bx1);
-            const int y0 = max((int)t.py0, (int)bi.y0), y1 = min((int)t.py1, by1);
-            if (x0 > x1 || y0 > y1) continue;
-            const long long dx0 = (long long)t.X1 - t.X0, dy0 = (long long)t.Y1 - t.Y0;
-            const long long dx1 = (long long)t.X2 - t.X1, dy1 = (long long)t.Y2 - t.Y1;
-            const long long dx2 = (long long)t.X0 - t.X2, dy2 = (long long)t.Y0 - t.Y2;
-            const bool tl0 = (t.Y1 < t.Y0) || (t.Y1 == t.Y0 && t.X1 < t.X0);
-            const bool tl1 = (t.Y2 < t.Y1) || (t.Y2 == t.Y1 && t.X2 < t.X1);
-            const bool tl2 = (t.Y0 < t.Y2) || (t.Y0 == t.Y2 && t.X0 < t.X2);
-            const int nsx = (x1 - x0 + 8) >> 3, nsy = (y1 - y0 + 4) >> 2;
-            for (int s = 0; s < nsx * nsy; s++) {
-                const int px = x0 + (s % nsx) * 8 + (lane & 7);
-                const int py = y0 + (s / nsx) * 4 + (lane >> 3);
-                if (px > x1 || py > y1) continue;
-                const long long PX = (long long)px * 256 + 128, PY = (long long)py * 256 + 128;
-                const long long e0 = dx0 * (PY - t.Y0) - dy0 * (PX - t.X0);
-                const long long e1 = dx1 * (PY - t.Y1) - dy1 * (PX - t.X1);
-                const long long e2 = dx2 * (PY - t.Y2) - dy2 * (PX - t.X2);
-                const bool in = (e0 > 0 || (e0 == 0 && tl0)) && (e1 > 0 || (e1 == 0 && tl1)) &&
-                                (e2 > 0 || (e2 == 0 && tl2));
-                if (!in) continue;
-                const float u = (float)(px - sx), w = (float)(py - sy);
-                const float D = (t.c0 + t.ax * u) + t.ay * w;
-                const unsigned long long k = ((unsigned long long)depth_ordinal(D) << 32) | t.id;
-                atomicMin(&key[(py - bi.y0) * TILE + (px - bi.x0)], k);
+        for (uint32_t base = 0; base < cnt; base += kChunk) {
+            const uint32_t m = min((uint32_t)kChunk, cnt - base);
+            if (threadIdx.x == 0) s_nbig = 0;
+            __syncthreads();
+            if (threadIdx.x < m) {
+                const TriRec& tr = b.tris[b.bin_list[off + base + threadIdx.x]];
+                const int4 a = *reinterpret_cast<const int4*>(&tr.X0);
+                const int4 c = *reinterpret_cast<const int4*>(&tr.X2);
+                const int4 d = *reinterpret_cast<const int4*>(&tr.ay);
+                RTri t;
+                t.X[0] = a.x; t.Y[0] = a.y; t.X[1] = a.z; t.Y[1] = a.w;
+                t.X[2] = c.x; t.Y[2] = c.y; t.c0 = __int_as_float(c.z); t.ax = __int_as_float(c.w);
+                t.ay = __int_as_float(d.x); t.id = (uint32_t)d.y;
+                const int px0 = (int)(int16_t)(d.z & 0xFFFF), px1 = (int)(int16_t)((uint32_t)d.z >> 16);
+                const int py0 = (int)(int16_t)(d.w & 0xFFFF), py1 = (int)(int16_t)((uint32_t)d.w >> 16);
+                const int x0 = max(px0, (int)bi.x0), x1 = min(px1, bx1);
+                const int y0 = max(py0, (int)bi.y0), y1 = min(py1, by1);
+                if (x0 <= x1 && y0 <= y1) {
+                    const int32_t ex = max(t.X[0], max(t.X[1], t.X[2])) - min(t.X[0], min(t.X[1], t.X[2]));
+                    const int32_t ey = max(t.Y[0], max(t.Y[1], t.Y[2])) - min(t.Y[0], min(t.Y[1], t.Y[2]));
+                    const int area = (x1 - x0 + 1) * (y1 - y0 + 1);
+                    if (ex <= kSmallExtent && ey <= kSmallExtent && area <= (int)g.small_max) {
+                        raster_small<TILE>(t, x0, x1, y0, y1, bi, sx, sy, key);
+                        if (ctr) {
+                            atomicAdd(&ctr[1], 1u);
+                            atomicAdd(&ctr[2], (uint32_t)area);
+                        }
+                    } else {
+                        s_big[atomicAdd(&s_nbig, 1)] = t;
+                        if (ctr) atomicAdd(&ctr[3], 1u);
+                    }
+                }
             }
+            __syncthreads();
+            const int nbig = s_nbig;
+            for (int i = warp; i < nbig; i += nwarp) {
+                const RTri t = s_big[i];
+                const int32_t xmn = min(t.X[0], min(t.X[1], t.X[2])), xmx = max(t.X[0], max(t.X[1], t.X[2]));
+                const int32_t ymn = min(t.Y[0], min(t.Y[1], t.Y[2])), ymx = max(t.Y[0], max(t.Y[1], t.Y[2]));
+                const int x0 = max((int)floordiv256((long long)xmn - 128 + 255), (int)bi.x0);
+                const int x1 = min((int)floordiv256((long long)xmx - 128), bx1);
+                const int y0 = max((int)floordiv256((long long)ymn - 128 + 255), (int)bi.y0);
+                const int y1 = min((int)floordiv256((long long)ymx - 128), by1);
+                if (x0 <= x1 && y0 <= y1) raster_big<TILE>(t, x0, x1, y0, y1, bi, sx, sy, key, lane, ctr);
+            }
+            __syncthreads();
         }
     }
     __syncthreads();
+    if (count && threadIdx.x < 8) {
+        uint32_t v = s_cnt[threadIdx.x];
+        if (threadIdx.x == 0) v = valid ? min(b.bin_count[gb], b.list_cap) : 0u;
+        if (v) atomicAdd(&st->raster_counters[threadIdx.x], (unsigned long long)v);
+    }
     const size_t img = (size_t)hi * g.RES;
+    uint32_t* h_id = reinterpret_cast<uint32_t*>(s_region);
+    unsigned long long* h_sum = reinterpret_cast<unsigned long long*>(s_region + 4 * kHashSlots);
+    if (fused) {
+        for (int j = threadIdx.x; j < kHashSlots; j += blockDim.x) {
+            h_id[j] = kHashEmpty;
+            h_sum[j] = 0;
+        }
+        __syncthreads();
+    }
+    unsigned long long* Fq = b.Fq + (size_t)hi * g.n;
     for (int j = threadIdx.x; j < TILE * TILE; j += blockDim.x) {
         const int ly = j / TILE, lx = j % TILE;
         const bool inb = lx < bi.w && ly < bi.h;
@@ -480,20 +683,55 @@ __global__ void __launch_bounds__(256) k_raster(Geo g, Batch b, const float* __r
         if (fused) {
             unsigned long long q = 0;
             if (has) q = __float2ull_rz(fftab[(size_t)py * g.TW + px] * 0x1p61f);
-            unsigned gm;
-            unsigned long long sum = group_sum(id, q, &gm);
-            if (has && lane == __ffs(gm) - 1) atomicAdd(&b.Fq[(size_t)hi * g.n + id], sum);
+            // runs of equal ids over consecutive lanes: exact sum per run with redux.sync
+            const uint32_t prev = __shfl_up_sync(0xffffffffu, id, 1);
+            const bool head = lane == 0 || prev != id;
+            const unsigned heads = __ballot_sync(0xffffffffu, head);
+            const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+            const int h = 31 - __clz(heads & upto);
+            const unsigned above = heads & ~upto;
+            const unsigned hi_mask = above ? ((1u << (__ffs(above) - 1)) - 1u) : 0xffffffffu;
+            const unsigned seg = hi_mask & ~((1u << h) - 1u);
+            const uint32_t a = (uint32_t)(q & 0x1FFFFFull), bb = (uint32_t)((q >> 21) & 0x1FFFFFull),
+                           c = (uint32_t)(q >> 42);
+            const uint32_t sa = __reduce_add_sync(seg, a), sb = __reduce_add_sync(seg, bb), sc = __reduce_add_sync(seg, c);
+            if (has && lane == h) {
+                const unsigned long long sum =
+                    (unsigned long long)sa + ((unsigned long long)sb << 21) + ((unsigned long long)sc << 42);
+                uint32_t slot = (id * 2654435761u) >> 22;
+                bool done = false;
+                for (int probe = 0; probe < 32 && !done; probe++) {
+                    uint32_t cur = h_id[slot];
+                    if (cur == kHashEmpty) {
+                        cur = atomicCAS(&h_id[slot], kHashEmpty, id);
+                        if (cur == kHashEmpty) cur = id;
+                    }
+                    if (cur == id) {
+                        atomicAdd(&h_sum[slot], sum);
+                        done = true;
+                    }
+                    slot = (slot + 1) & (kHashSlots - 1);
+                }
+                if (!done) atomicAdd(&Fq[id], sum);  // table crowded: straight to the global sum
+            }
+        }
+    }
+    if (fused) {
+        __syncthreads();
+        for (int j = threadIdx.x; j < kHashSlots; j += blockDim.x) {
+            const uint32_t id = h_id[j];
+            if (id != kHashEmpty) atomicAdd(&Fq[id], h_sum[j]);
         }
     }
 }
 
 void launch_raster(const Geo& g, const Batch& b, const float* fftab, DevState* st, bool write_items,
-                   bool fused_reduce, cudaStream_t s) {
+                   bool fused_reduce, cudaStream_t s, bool count) {
     dim3 grid(b.K * g.nb);
     switch (g.tile) {
-        case 16: k_raster<16><<<grid, 256, 0, s>>>(g, b, fftab, st, write_items, fused_reduce); break;
-        case 64: k_raster<64><<<grid, 256, 0, s>>>(g, b, fftab, st, write_items, fused_reduce); break;
-        default: k_raster<32><<<grid, 256, 0, s>>>(g, b, fftab, st, write_items, fused_reduce); break;
+        case 16: k_raster<16><<<grid, 256, 0, s>>>(g, b, fftab, st, write_items, fused_reduce, count); break;
+        case 64: k_raster<64><<<grid, 256, 0, s>>>(g, b, fftab, st, write_items, fused_reduce, count); break;
+        default: k_raster<32><<<grid, 256, 0, s>>>(g, b, fftab, st, write_items, fused_reduce, count); break;
     }
 }
 

@@ -14,7 +14,7 @@
 #include <cstring>
 #include <vector>
 
-#include "../../include/radiosity.h"
+#include "radiosity.h"
 
 namespace {
 

@@ -214,9 +214,194 @@ __global__ void __launch_bounds__(kSelThreads) k_select(Geo g, Batch b, const fl
     }
 }
 
+// ---------------------------------------------------------------------------
+// PHYS selection: K largest unshot powers, ties to the lower index.  Keys are the
+// float bits of the power (monotonic for positives); composites
+// (key << 32 | ~index) are unique and order exactly as required.  A 2048-bin
+// histogram of the top 12 key bits finds the boundary bin; elements above it
+// are selected outright, the boundary bin is refined by an exact radix select
+// on the composites in one CTA, and the K winners are bitonic-sorted.
+// ---------------------------------------------------------------------------
+constexpr int kHist = 2048;
+
+__global__ void __launch_bounds__(256) k_psel_hist(Geo g, Batch b, const float4* __restrict__ rad,
+                                                   const float* __restrict__ area, DevState* st) {
+    if (st->stopped) return;
+    __shared__ uint32_t h[kHist];
+    for (int i = threadIdx.x; i < kHist; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
+        const float v = sel_value(1, rad[i], area[i]);
+        const uint32_t bits = v > 0 ? __float_as_uint(v) : 0u;
+        b.sel_keys[i] = bits;
+        if (bits) atomicAdd(&h[bits >> 20], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kHist; i += blockDim.x)
+        if (h[i]) atomicAdd(&b.sel_hist[i], h[i]);
+}
+
+__global__ void __launch_bounds__(1024) k_psel_pick(Batch b, DevState* st) {
+    if (st->stopped) return;
+    __shared__ uint32_t suf[kHist + 1];
+    __shared__ uint32_t part[1024];
+    const int t = threadIdx.x;
+    // suffix sums: element r of the reversed histogram is bin kHist-1-r
+    const uint32_t a0 = b.sel_hist[kHist - 1 - 2 * t], a1 = b.sel_hist[kHist - 2 - 2 * t];
+    part[t] = a0 + a1;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const uint32_t v = t >= o ? part[t - o] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    const uint32_t before = part[t] - (a0 + a1);
+    suf[kHist - 1 - 2 * t] = before + a0;
+    suf[kHist - 2 - 2 * t] = before + a0 + a1;
+    if (t == 0) suf[kHist] = 0;
+    __syncthreads();
+    const uint32_t K = b.K, total = suf[0];
+    for (int i = t; i < kHist; i += blockDim.x) {
+        const bool pick = total < K ? (i == 0) : (suf[i] >= K && suf[i + 1] < K);
+        if (pick) {
+            b.sel_ctrl[0] = (uint32_t)i;
+            b.sel_ctrl[1] = suf[i + 1];
+        }
+    }
+    if (t == 0) {
+        b.sel_ctrl[2] = 0;
+        b.sel_ctrl[3] = 0;
+        b.sel_ctrl[4] = total;
+    }
+    __syncthreads();
+    for (int i = t; i < kHist; i += blockDim.x) b.sel_hist[i] = 0;  // ready for the next batch
+}
+
+__global__ void __launch_bounds__(256) k_psel_collect(Geo g, Batch b, DevState* st) {
+    if (st->stopped) return;
+    const uint32_t B = b.sel_ctrl[0];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
+        const uint32_t bits = b.sel_keys[i];
+        if (!bits) continue;
+        const uint32_t bin = bits >> 20;
+        if (bin < B) continue;
+        const unsigned long long comp = ((unsigned long long)bits << 32) | (0xFFFFFFFFu - i);
+        if (bin > B) {
+            const uint32_t pos = atomicAdd(&b.sel_ctrl[2], 1u);
+            if (pos < b.K) b.sel_sure[pos] = comp;
+        } else {
+            const uint32_t pos = atomicAdd(&b.sel_ctrl[3], 1u);
+            if (pos < g.n) b.sel_bnd[pos] = comp;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_psel_final(Geo g, Batch b, DevState* st) {
+    if (st->stopped) return;
+    __shared__ uint32_t hist[256];
+    __shared__ unsigned long long arr[kMaxK];
+    __shared__ unsigned long long s_prefix, s_mask;
+    __shared__ uint32_t s_rem, s_cnt;
+    const int t = threadIdx.x;
+    const uint32_t K = b.K, n_sure = min(b.sel_ctrl[2], K), n_bnd = min(b.sel_ctrl[3], g.n);
+    const uint32_t take = min(K, b.sel_ctrl[4]);
+    const uint32_t R = take > n_sure ? take - n_sure : 0u;
+    if (t == 0) {
+        s_prefix = 0;
+        s_mask = 0;
+        s_rem = R;
+        s_cnt = 0;
+    }
+    __syncthreads();
+    // Boundary elements share the top 12 composite bits (their histogram bin); an
+    // exact radix select over the low 52 bits (digits of 8,8,8,8,8,8,4 bits) finds
+    // the R-th largest composite, so exactly R boundary elements are >= thr.
+    unsigned long long thr = 0;
+    if (R < n_bnd) {
+        const int shifts[7] = {44, 36, 28, 20, 12, 4, 0};
+        for (int d = 0; d < 7; d++) {
+            const int sh = shifts[d];
+            const unsigned long long dmask = d < 6 ? 0xFFull : 0xFull;
+            for (int i = t; i < 256; i += blockDim.x) hist[i] = 0;
+            __syncthreads();
+            const unsigned long long pm = s_mask, pv = s_prefix;
+            for (uint32_t j = t; j < n_bnd; j += blockDim.x) {
+                const unsigned long long c = b.sel_bnd[j];
+                if ((c & pm) == pv) atomicAdd(&hist[(c >> sh) & dmask], 1u);
+            }
+            __syncthreads();
+            if (t == 0) {
+                uint32_t cum = 0;
+                const uint32_t rem = s_rem;
+                for (int v = (int)dmask; v >= 0; v--) {
+                    if (cum + hist[v] >= rem) {
+                        s_rem = rem - cum;
+                        s_prefix = pv | ((unsigned long long)v << sh);
+                        s_mask = pm | (dmask << sh);
+                        break;
+                    }
+                    cum += hist[v];
+                }
+            }
+            __syncthreads();
+        }
+        thr = s_prefix;
+    }
+    // gather the winners
+    for (uint32_t j = t; j < n_sure; j += blockDim.x) arr[j] = b.sel_sure[j];
+    __syncthreads();
+    const unsigned long long lowmask = 0x000FFFFFFFFFFFFFull;
+    for (uint32_t j = t; j < n_bnd; j += blockDim.x) {
+        const unsigned long long c = b.sel_bnd[j];
+        if (R >= n_bnd || (c & lowmask) >= thr) {
+            const uint32_t pos = n_sure + atomicAdd(&s_cnt, 1u);
+            if (pos < K) arr[pos] = c;
+        }
+    }
+    __syncthreads();
+    uint32_t P = 32;
+    while (P < take) P <<= 1;
+    for (uint32_t j = take + t; j < P; j += blockDim.x) arr[j] = 0;
+    __syncthreads();
+    for (uint32_t k = 2; k <= P; k <<= 1)
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = t; i < P; i += blockDim.x) {
+                const uint32_t ixj = i ^ j;
+                if (ixj > i) {
+                    const unsigned long long a = arr[i], c = arr[ixj];
+                    const bool desc = (i & k) == 0;
+                    if (desc ? (a < c) : (a > c)) {
+                        arr[i] = c;
+                        arr[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (uint32_t k = t; k < K; k += blockDim.x) {
+        if (k < take) {
+            b.shooters[k] = 0xFFFFFFFFu - (uint32_t)(arr[k] & 0xFFFFFFFFull);
+            b.valid[k] = 1;
+        } else {
+            b.shooters[k] = 0;
+            b.valid[k] = 0;
+        }
+    }
+}
+
 void launch_select(const Geo& g, const Batch& b, const float4* rad, const float* area, DevState* st,
                    cudaStream_t s) {
-    k_select<<<1, kSelThreads, 0, s>>>(g, b, rad, area, st);
+    if (g.mode == 0) {
+        k_select<<<1, kSelThreads, 0, s>>>(g, b, rad, area, st);
+        return;
+    }
+    uint32_t blocks = (g.n + 255) / 256;
+    if (blocks > 152 * 4) blocks = 152 * 4;
+    k_psel_hist<<<blocks, 256, 0, s>>>(g, b, rad, area, st);
+    k_psel_pick<<<1, 1024, 0, s>>>(b, st);
+    k_psel_collect<<<blocks, 256, 0, s>>>(g, b, st);
+    k_psel_final<<<1, 1024, 0, s>>>(g, b, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -243,6 +428,7 @@ __global__ void __launch_bounds__(256) k_update(Geo g, Batch b, const float4* __
     }
     __syncthreads();
     const uint32_t N = g.n;
+    double acc = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
         float4 r = rad[i];
         if (g.mode == 0) {
@@ -279,15 +465,29 @@ __global__ void __launch_bounds__(256) k_update(Geo g, Batch b, const float4* __
             }
         }
         rad[i] = r;
+        if (g.mode != 0) acc += (double)area[i] * (((double)r.x + (double)r.y) + (double)r.z);
     }
+    if (g.mode != 0) {  // FP64 partial of the unshot power after the update (residual)
+        __shared__ double red[256];
+        red[threadIdx.x] = acc;
+        __syncthreads();
+        for (uint32_t o = blockDim.x / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) b.partials[blockIdx.x] = red[0];
+    }
+}
+
+static uint32_t update_blocks(uint32_t n) {
+    uint32_t blocks = (n + 255) / 256;
+    if (blocks > (uint32_t)kUpdateBlocks) blocks = kUpdateBlocks;
+    return blocks ? blocks : 1;
 }
 
 void launch_update(const Geo& g, const Batch& b, const float4* color, const float4* rho, const float* area,
                    float4* rad, DevState* st, cudaStream_t s) {
-    uint32_t blocks = (g.n + 255) / 256;
-    if (blocks > 152 * 8) blocks = 152 * 8;
-    if (blocks == 0) blocks = 1;
-    k_update<<<blocks, 256, 0, s>>>(g, b, color, rho, area, rad, st);
+    k_update<<<update_blocks(g.n), 256, 0, s>>>(g, b, color, rho, area, rad, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -311,47 +511,70 @@ __device__ double block_unshot_power(const float4* __restrict__ rad, const float
     return r;
 }
 
+// Emitters of one batch are distinct patches, so their updates run in parallel;
+// lastEnergy is the pre-subtraction radiosity of the last valid emitter.
 __global__ void __launch_bounds__(256) k_emitters(Geo g, Batch b, float4* __restrict__ rad,
                                                   float4* __restrict__ illum, const float* __restrict__ area,
-                                                  double tol, DevState* st) {
+                                                  double tol, uint32_t nparts, DevState* st) {
     if (st->stopped) return;
     __shared__ double red[256];
-    __shared__ int s_stop;
+    __shared__ int s_last;
+    __shared__ uint32_t s_nv;
     if (threadIdx.x == 0) {
-        float4 last = make_float4(0, 0, 0, 0);
-        uint32_t nv = 0;
-        for (uint32_t h = 0; h < b.K; h++) {
-            if (!b.valid[h]) continue;
-            nv++;
-            const uint32_t e = b.shooters[h];
-            float4 r = rad[e], il = illum[e];
-            const float4 s = b.saved[h];
-            last = r;
-            il.x = il.x + s.x; il.y = il.y + s.y; il.z = il.z + s.z;
-            r.x = r.x - s.x; r.y = r.y - s.y; r.z = r.z - s.z;
-            rad[e] = r;
-            illum[e] = il;
-        }
-        st->shots_done += 1;
-        st->hemicubes += (double)nv;
-        st->last_energy[0] = last.x;
-        st->last_energy[1] = last.y;
-        st->last_energy[2] = last.z;
-        int stop = 0;
-        if (g.mode == 0) stop = (double)sqrtf(last.x * last.x + last.y * last.y + last.z * last.z) < 0.1;
-        s_stop = stop;
+        s_last = -1;
+        s_nv = 0;
     }
     __syncthreads();
-    int stop = s_stop;
+    uint32_t nv = 0;
+    for (uint32_t h = threadIdx.x; h < b.K; h += blockDim.x)
+        if (b.valid[h]) {
+            atomicMax(&s_last, (int)h);
+            nv++;
+        }
+    atomicAdd(&s_nv, nv);
+    __syncthreads();
+    const int last = s_last;
+    double corr = 0;
+    for (uint32_t h = threadIdx.x; h < b.K; h += blockDim.x) {
+        if (!b.valid[h]) continue;
+        const uint32_t e = b.shooters[h];
+        float4 r = rad[e], il = illum[e];
+        const float4 sv = b.saved[h];
+        if ((int)h == last) {
+            st->last_energy[0] = r.x;
+            st->last_energy[1] = r.y;
+            st->last_energy[2] = r.z;
+            if (g.mode == 0) {
+                const bool stop = (double)sqrtf(r.x * r.x + r.y * r.y + r.z * r.z) < 0.1;
+                if (stop) st->stopped = 1;
+            }
+        }
+        if (g.mode != 0) corr -= (double)area[e] * (((double)r.x + (double)r.y) + (double)r.z);
+        il.x = il.x + sv.x; il.y = il.y + sv.y; il.z = il.z + sv.z;
+        r.x = r.x - sv.x; r.y = r.y - sv.y; r.z = r.z - sv.z;
+        if (g.mode != 0) corr += (double)area[e] * (((double)r.x + (double)r.y) + (double)r.z);
+        rad[e] = r;
+        illum[e] = il;
+    }
+    if (threadIdx.x == 0) {
+        st->shots_done += 1;
+        st->hemicubes += (double)s_nv;
+    }
     if (g.mode != 0) {
-        const double p = block_unshot_power(rad, area, g.n, red);
+        double p = corr;
+        for (uint32_t i = threadIdx.x; i < nparts; i += blockDim.x) p += b.partials[i];
+        red[threadIdx.x] = p;
+        __syncthreads();
+        for (uint32_t o = blockDim.x / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+            __syncthreads();
+        }
         if (threadIdx.x == 0) {
-            const double res = st->power0 > 0 ? p / st->power0 : 0.0;
+            const double res = st->power0 > 0 ? red[0] / st->power0 : 0.0;
             st->residual = res;
-            if (res <= tol) stop = 1;
+            if (res <= tol) st->stopped = 1;
         }
     }
-    if (threadIdx.x == 0 && stop) st->stopped = 1;
 }
 
 __global__ void __launch_bounds__(256) k_power0(const float4* __restrict__ rad, const float* __restrict__ area,
@@ -367,7 +590,7 @@ __global__ void __launch_bounds__(256) k_power0(const float4* __restrict__ rad, 
 void launch_emitters(const Geo& g, const Batch& b, float4* rad, float4* illum, const float* area, double tol,
                      double* partials, DevState* st, cudaStream_t s) {
     (void)partials;
-    k_emitters<<<1, 256, 0, s>>>(g, b, rad, illum, area, tol, st);
+    k_emitters<<<1, 256, 0, s>>>(g, b, rad, illum, area, tol, update_blocks(g.n), st);
 }
 
 void launch_power0(const float4* rad, const float* area, uint32_t n, DevState* st, cudaStream_t s) {

@@ -133,7 +133,7 @@ def test_select_ref_random_large(lib, orc, cornell, K):
             assert np.array_equal(v, rv) and np.array_equal(i[v], ri[rv])
 
 
-@pytest.mark.parametrize("K", [1, 8, 33])
+@pytest.mark.parametrize("K", [1, 8, 33, 128, 512])
 def test_select_phys(lib, orc, room, K):
     rng = np.random.default_rng(100 + K)
     n = room["n"]
@@ -251,3 +251,31 @@ def test_full_size_properties(lib):
         r2, i2 = s.download()
     assert np.array_equal(_bits(r1), _bits(r2)) and np.array_equal(_bits(i1), _bits(i2))
     assert st1.residual == st2.residual and 0 < st1.residual < 1
+
+
+def test_autotune_keeps_results_bit_exact(lib, orc, room):
+    """The autotuner only changes the raster's bin side and lane/warp split: results stay bit-exact."""
+    W, K, S = 64, 16, 6
+    with solver(lib, room, W, K, mode=1) as s:
+        t = s.autotune(tune_k=False)
+        assert t.tile in (16, 32, 64) and t.small_tri_pixels in (16, 32, 64, 128, 256) and t.candidates >= 10
+        assert t.hemicubes_count == K and t.us_per_hemicube > 0
+        st = s.shoot(S)
+        rad, ill = s.download()
+    orad, oill, _ = orc.shoot(1, W, K, room["vertices"], room["color"], room["radiosity"], room["illumination"], S,
+                              rho=room["reflectance"])
+    assert st.shots_done == S
+    assert np.array_equal(_bits(rad), _bits(orad)) and np.array_equal(_bits(ill), _bits(oill))
+
+
+@pytest.mark.parametrize("small", [1, 16, 256, 4096])
+def test_lane_warp_split_is_exact(lib, orc, cornell, small):
+    W, n = 128, cornell["n"]
+    sh = np.array([int(light_ids(cornell)[1]), 33, 2048, 5100], np.uint32)
+    with solver(lib, cornell, W, 4, tile=32, small_tri_pixels=small) as s:
+        F = s.ff_rows(sh)
+        s.profile_stages(1)
+        c = s.raster_counters()
+    assert c["pairs"] > 0 and c["small_tris"] + c["big_tris"] <= c["pairs"]
+    items = np.concatenate([orc.render(W, cornell["vertices"], int(p)) for p in sh])
+    assert np.array_equal(_bits(F), _bits(orc.ff_exact(W, items, len(sh), n)))
