@@ -143,6 +143,43 @@ typedef struct rad_tuning {
  * not modified.  out may be NULL. */
 int rad_autotune(rad_ctx* ctx, uint32_t flags, rad_tuning* out);
 
+/* ---- Precision form: dense form factors and the gathering solve ---------------------
+ * No counterpart in the reference (its solve is progressive shooting only): the rows of
+ * the form-factor matrix are captured with the same hemicube pipeline (one hemicube per
+ * patch), stored as BF16 with one FP32 scale per row (and optionally FP32), and
+ * B = E + rho o (F B) is solved by mixed-precision iterative refinement: FP32 residuals,
+ * BF16 Jacobi sweeps of the correction on tcgen05 tensor cores (FP32 accumulation),
+ * FP64 norms.  rho is the scene's reflectance (PHYS mode). */
+#define RAD_DENSE_FP32 1u /* also keep FP32 rows: needed by rad_gather_solve */
+
+/* Captures every row of F (N hemicubes).  device_ms may be NULL. */
+int rad_dense_capture(rad_ctx* ctx, uint32_t flags, double* device_ms);
+
+/* Copies rows [first, first+count) of the captured matrix: FP32 (count x N), the BF16
+ * bits (count x N) and the row scales (count); any output may be NULL. */
+int rad_dense_rows(rad_ctx* ctx, uint32_t first, uint32_t count, float* f32, uint16_t* bf16, float* scale);
+
+typedef struct rad_gather_stats {
+    uint32_t outer;           /* FP32 residual evaluations */
+    uint32_t sweeps;          /* BF16 tcgen05 sweeps */
+    double initial_residual;  /* max over columns of ||r_c||_2 / ||E_c||_2 at the guess */
+    double residual;          /* the same at return */
+    double device_ms;         /* whole solve, CUDA events */
+    double sweep_ms;          /* inside the tcgen05 sweeps */
+    double resid_ms;          /* inside the FP32 residual GEMMs */
+} rad_gather_stats;
+
+/* Solves B = E + rho o (F B) for R <= 256 right-hand sides, column-major N x R host
+ * arrays (column c uses reflectance channel c % 3).  guess may be NULL (start from E).
+ * Stops when the relative residual <= tol or after max_outer refinements; each
+ * refinement runs `sweeps` BF16 sweeps.  Needs rad_dense_capture(RAD_DENSE_FP32). */
+int rad_gather_solve(rad_ctx* ctx, const float* emission, uint32_t R, const float* guess, double tol,
+                     uint32_t max_outer, uint32_t sweeps, float* radiosity, rad_gather_stats* stats);
+
+/* Diagnostic: C = A * Bt^T on the tcgen05 path (A n x k, Bt R x k BF16 bits, row-major;
+ * C column-major R x n FP32), on `device`. */
+int rad_bf16_gemm(int device, const uint16_t* A, const uint16_t* Bt, uint32_t n, uint32_t k, uint32_t R, float* C);
+
 /* Raster counters of the last rad_profile_stages call (8 values): triangle-bin pairs,
  * small triangles (one lane each), their bbox pixels, large triangles (one warp each),
  * their 8x4 stamps, stamps visited, stamps wholly inside, large-triangle pixels written. */

@@ -6,7 +6,8 @@ with ctypes.  Scene generators for the synthetic benchmark workloads live in
 ``radiosity_gb300.scenes``.
 """
 from ._lib import (  # noqa: F401
-    EXPORTS, MODE_PHYS, MODE_REF, RadConfig, RadError, RadStats, RadTuning, Solver, default_config, derived, load,
+    EXPORTS, MODE_PHYS, MODE_REF, RadConfig, RadError, RadGatherStats, RadStats, RadTuning, Solver, bf16_gemm,
+    default_config, derived, load,
     reference_scene,
 )
 from .build import LIB as LIB_PATH  # noqa: F401

@@ -32,7 +32,8 @@ EXPORTS = [
     "rad_config_default", "rad_config_derived", "rad_create", "rad_destroy", "rad_upload_scene",
     "rad_set_state", "rad_download", "rad_ff_table", "rad_select_shooters", "rad_render_item_buffers",
     "rad_reduce_item_buffers", "rad_ff_rows", "rad_shoot", "rad_profile_stages", "rad_scene_reference",
-    "rad_reduce_items_noalloc", "rad_raster_counters", "rad_autotune", "rad_strerror", "rad_last_error",
+    "rad_reduce_items_noalloc", "rad_raster_counters", "rad_autotune", "rad_dense_capture",
+    "rad_dense_rows", "rad_gather_solve", "rad_bf16_gemm", "rad_strerror", "rad_last_error",
 ]
 STAGES = ["select", "camera", "setup", "bins", "raster", "update", "emitters"]
 STAGE_KERNELS = [1, 1, 1, 2, 1, 1, 1]
@@ -52,6 +53,18 @@ class RadConfig(ctypes.Structure):
         ("binref_capacity", ctypes.c_uint32),
         ("device", ctypes.c_int32),
         ("small_tri_pixels", ctypes.c_uint32),
+    ]
+
+
+class RadGatherStats(ctypes.Structure):
+    _fields_ = [
+        ("outer", ctypes.c_uint32),
+        ("sweeps", ctypes.c_uint32),
+        ("initial_residual", ctypes.c_double),
+        ("residual", ctypes.c_double),
+        ("device_ms", ctypes.c_double),
+        ("sweep_ms", ctypes.c_double),
+        ("resid_ms", ctypes.c_double),
     ]
 
 
@@ -111,6 +124,11 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rad_shoot.argtypes = [vp, ctypes.c_uint32, P(RadStats)]
     L.rad_profile_stages.argtypes = [vp, ctypes.c_uint32, np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS"),
                                      P(RadStats)]
+    L.rad_dense_capture.argtypes = [vp, ctypes.c_uint32, P(ctypes.c_double)]
+    L.rad_dense_rows.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, vp, vp, vp]
+    L.rad_gather_solve.argtypes = [vp, _f32p, ctypes.c_uint32, vp, ctypes.c_double, ctypes.c_uint32,
+                                   ctypes.c_uint32, _f32p, P(RadGatherStats)]
+    L.rad_bf16_gemm.argtypes = [ctypes.c_int, vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _f32p]
     L.rad_autotune.argtypes = [vp, ctypes.c_uint32, P(RadTuning)]
     L.rad_raster_counters.argtypes = [vp, np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")]
     L.rad_reduce_items_noalloc.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp, vp]
@@ -153,6 +171,20 @@ def reference_scene(max_patch_area: float) -> dict:
         raise RadError(rc, "rad_scene_reference")
     out["n"] = N
     return out
+
+
+def bf16_gemm(A_bits: np.ndarray, Bt_bits: np.ndarray, device: int = 0) -> np.ndarray:
+    """rad_bf16_gemm: C (R x n, column-major rows of C^T) = A (n x k) * Bt (R x k)^T on tcgen05."""
+    L = load()
+    A = np.ascontiguousarray(A_bits, np.uint16)
+    B = np.ascontiguousarray(Bt_bits, np.uint16)
+    n, k = A.shape
+    R = B.shape[0]
+    C = np.zeros(R * n, np.float32)
+    rc = L.rad_bf16_gemm(device, A.ctypes.data_as(ctypes.c_void_p), B.ctypes.data_as(ctypes.c_void_p), n, k, R, C)
+    if rc:
+        raise RadError(rc, L.rad_strerror(rc).decode())
+    return C.reshape(R, n)
 
 
 def default_config(**kw) -> RadConfig:
@@ -278,6 +310,30 @@ class Solver:
         self.cfg.small_tri_pixels = t.small_tri_pixels
         self.cfg.hemicubes_count = t.hemicubes_count
         return t
+
+    def dense_capture(self, keep_fp32: bool = True) -> float:
+        """rad_dense_capture: every form-factor row; returns device ms."""
+        ms = ctypes.c_double()
+        self._check(self.L.rad_dense_capture(self.h, 1 if keep_fp32 else 0, ctypes.byref(ms)), "rad_dense_capture")
+        return ms.value
+
+    def dense_rows(self, first: int, count: int):
+        f = np.zeros(count * self.n, np.float32)
+        h = np.zeros(count * self.n, np.uint16)
+        sc = np.zeros(count, np.float32)
+        self._check(self.L.rad_dense_rows(self.h, first, count, _ptr(f), _ptr(h), _ptr(sc)), "rad_dense_rows")
+        return f.reshape(count, self.n), h.reshape(count, self.n), sc
+
+    def gather(self, emission, guess=None, tol: float = 1e-6, max_outer: int = 50, sweeps: int = 8):
+        """rad_gather_solve on column-major N x R blocks (given as R x N arrays)."""
+        E = np.ascontiguousarray(emission, np.float32)
+        R = E.shape[0]
+        out = np.zeros_like(E)
+        st = RadGatherStats()
+        g = None if guess is None else np.ascontiguousarray(guess, np.float32)
+        self._check(self.L.rad_gather_solve(self.h, E.reshape(-1), R, _ptr(g), tol, max_outer, sweeps,
+                                            out.reshape(-1), ctypes.byref(st)), "rad_gather_solve")
+        return out, st
 
     RASTER_COUNTERS = ["pairs", "small_tris", "small_px", "big_tris", "big_stamps", "stamps_visited",
                        "stamps_inside", "big_px_written"]

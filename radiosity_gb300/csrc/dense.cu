@@ -1,0 +1,412 @@
+// Dense form-factor capture and the gathering solve B = E + rho o (F B).
+//
+// F rows come from the hemicube pipeline (exact sums, one row per shooter).  They
+// are kept as FP32 rows and as BF16 rows with one FP32 scale per row
+// (F_ij ~= scale_i * bf16_ij, scale_i = max_j F_ij).  The solve is mixed-precision
+// iterative refinement:
+//     r  = E + rho o (F32 B) - B                     FP32 GEMM (k_sgemm_resid), FP64 norms
+//     d <- r + rho o (scale o (F16 d))   (m sweeps)  BF16 tcgen05 GEMM (k_gemm_tc)
+//     B <- B + d
+// Right-hand sides are column-major: column c of an N x R block is contiguous, and
+// column c uses the reflectance channel c % 3.
+//
+// k_gemm_tc is a warp-specialised tcgen05 GEMM for C[128 x NR] tiles: warp 0 issues
+// TMA loads (128B swizzle) of a 128 x 64 tile of F16 and an NR x 64 tile of the
+// transposed operand into a 4-stage ring, warp 1 issues tcgen05.mma (BF16 x BF16 ->
+// FP32 in TMEM) and frees stages with tcgen05.commit, warp 2 owns the TMEM
+// allocation, and warps 4-7 read the accumulator with tcgen05.ld and run the fused
+// epilogue.  Every mbarrier wait is bounded by wall-clock time; a timeout sets the
+// error word and the kernel drains and frees its TMEM before returning.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "rad_internal.cuh"
+
+namespace rad {
+
+// ---------------------------------------------------------------------------
+// Row capture: exact sums -> FP32 rows, BF16 rows + per-row scale
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_dense_rows(const unsigned long long* __restrict__ Fq, uint32_t n, uint32_t ld,
+                                                    uint32_t first, float* F32, __nv_bfloat16* F16, float* scale) {
+    const uint32_t r = blockIdx.x;  // row within the batch
+    const unsigned long long* src = Fq + (size_t)r * n;
+    const size_t row = (size_t)(first + r);
+    __shared__ float red[256];
+    float mx = 0.f;
+    for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
+        const float f = __ull2float_rn(src[j]) * 0x1p-61f;
+        if (F32) F32[row * ld + j] = f;
+        mx = fmaxf(mx, f);
+    }
+    red[threadIdx.x] = mx;
+    __syncthreads();
+    for (uint32_t o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + o]);
+        __syncthreads();
+    }
+    const float s = red[0] > 0.f ? red[0] : 1.0f;
+    const float inv = 1.0f / s;
+    for (uint32_t j = threadIdx.x; j < ld; j += blockDim.x) {
+        const float f = j < n ? __ull2float_rn(src[j]) * 0x1p-61f : 0.f;
+        F16[row * ld + j] = __float2bfloat16_rn(f * inv);
+    }
+    if (threadIdx.x == 0) scale[row] = s;
+}
+
+void launch_dense_rows(const unsigned long long* Fq, uint32_t count, uint32_t n, uint32_t ld, uint32_t first,
+                       float* F32, __nv_bfloat16* F16, float* scale, cudaStream_t s) {
+    k_dense_rows<<<count, 256, 0, s>>>(Fq, n, ld, first, F32, F16, scale);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 residual GEMM: r[c][i] = E[c][i] + rho_i[c%3] * sum_j F[i][j] X[c][j] - X[c][i]
+// 64 (rows) x 64 (columns) tiles, 16-deep k slabs, 4x4 outputs per thread.
+// Column norms: nrm[c] += r^2 (FP64 atomics).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_sgemm_resid(const float* __restrict__ F, uint32_t n, uint32_t ld,
+                                                     const float* __restrict__ X, const float* __restrict__ E,
+                                                     const float4* __restrict__ rho, uint32_t R, float* r,
+                                                     double* nrm) {
+    __shared__ float As[16][64 + 4];
+    __shared__ float Bs[16][64 + 4];
+    const uint32_t i0 = blockIdx.x * 64, c0 = blockIdx.y * 64;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    float acc[4][4] = {};
+    for (uint32_t k0 = 0; k0 < n; k0 += 16) {
+        for (int e = threadIdx.x; e < 64 * 16; e += 256) {
+            const int rr = e >> 4, kk = e & 15;
+            const uint32_t gi = i0 + rr, gk = k0 + kk, gc = c0 + rr;
+            As[kk][rr] = (gi < n && gk < n) ? F[(size_t)gi * ld + gk] : 0.f;
+            Bs[kk][rr] = (gc < R && gk < n) ? X[(size_t)gc * n + gk] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < 16; kk++) {
+            float a[4], bb[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                a[q] = As[kk][ty * 4 + q];
+                bb[q] = Bs[kk][tx * 4 + q];
+            }
+#pragma unroll
+            for (int p = 0; p < 4; p++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) acc[p][q] = fmaf(a[p], bb[q], acc[p][q]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const uint32_t c = c0 + tx * 4 + q;
+        double part = 0;
+        if (c < R) {
+#pragma unroll
+            for (int p = 0; p < 4; p++) {
+                const uint32_t i = i0 + ty * 4 + p;
+                if (i >= n) continue;
+                const float4 rh = rho[i];
+                const int ch = (int)(c % 3);
+                const float rr = ch == 0 ? rh.x : (ch == 1 ? rh.y : rh.z);
+                const float v = E[(size_t)c * n + i] + rr * acc[p][q] - X[(size_t)c * n + i];
+                r[(size_t)c * n + i] = v;
+                part += (double)v * (double)v;
+            }
+            if (nrm) atomicAdd(&nrm[c], part);
+        }
+    }
+}
+
+void launch_sgemm_resid(const float* F, uint32_t n, uint32_t ld, const float* X, const float* E, const float4* rho,
+                        uint32_t R, float* r, double* nrm, cudaStream_t s) {
+    dim3 grid((n + 63) / 64, (R + 63) / 64);
+    k_sgemm_resid<<<grid, 256, 0, s>>>(F, n, ld, X, E, rho, R, r, nrm);
+}
+
+// BF16 transposed copy of a column-major N x R block: Xt[c][j] (ld columns, zero padded).
+__global__ void k_pack_bf16(const float* __restrict__ X, uint32_t n, uint32_t R, uint32_t ld, __nv_bfloat16* Xt,
+                            uint32_t Rpad) {
+    const size_t total = (size_t)Rpad * ld;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t c = (uint32_t)(e / ld), j = (uint32_t)(e % ld);
+        Xt[e] = __float2bfloat16_rn((c < R && j < n) ? X[(size_t)c * n + j] : 0.f);
+    }
+}
+
+void launch_pack_bf16(const float* X, uint32_t n, uint32_t R, uint32_t ld, __nv_bfloat16* Xt, uint32_t Rpad,
+                      cudaStream_t s) {
+    k_pack_bf16<<<152 * 8, 256, 0, s>>>(X, n, R, ld, Xt, Rpad);
+}
+
+__global__ void k_axpy(float* __restrict__ y, const float* __restrict__ x, size_t total) {
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x)
+        y[e] = y[e] + x[e];
+}
+
+void launch_axpy(float* y, const float* x, size_t total, cudaStream_t s) { k_axpy<<<152 * 8, 256, 0, s>>>(y, x, total); }
+
+// ---------------------------------------------------------------------------
+// tcgen05 BF16 GEMM
+// ---------------------------------------------------------------------------
+constexpr int kTcM = 128, kTcBK = 64, kTcStages = 4;
+constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s bound on every wait
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+
+// Waits for the phase of the given parity; false (and the error word set) after kWaitNs.
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, uint32_t* err) {
+    const uint32_t a = smem_u32(b);
+    unsigned long long t0 = 0;
+    for (uint32_t it = 0;; it++) {
+        uint32_t done;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if ((it & 255u) == 0) {
+            const unsigned long long t = global_ns();
+            if (it == 0) t0 = t;
+            else if (t - t0 > kWaitNs) {
+                atomicOr(err, 1u);
+                return false;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128B swizzle, 8-row groups 1024 B apart.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;            // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset
+    d |= (uint64_t)1 << 46;            // descriptor version
+    d |= (uint64_t)2 << 61;            // SWIZZLE_128B
+    return d;
+}
+
+template <int NR>
+struct TcShape {
+    static constexpr uint32_t kA = kTcM * kTcBK * 2;
+    static constexpr uint32_t kB = NR * kTcBK * 2;
+    static constexpr uint32_t kStage = kA + kB;
+    static constexpr uint32_t kCols = NR <= 32 ? 32 : (NR <= 64 ? 64 : (NR <= 128 ? 128 : 256));
+    static constexpr uint32_t kSmem = kTcStages * kStage + 1024 + 256;
+    // instruction descriptor: D f32, A/B bf16, K-major both, N = NR, M = 128
+    static constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NR >> 3) << 17) |
+                                       ((uint32_t)(kTcM >> 4) << 24);
+};
+
+template <int NR>
+__global__ void __launch_bounds__(256, 1) k_gemm_tc(const __grid_constant__ CUtensorMap tmA,
+                                                    const __grid_constant__ CUtensorMap tmB, uint32_t kblocks,
+                                                    TcEpilogue ep) {
+    using S = TcShape<NR>;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + kTcStages * S::kStage);
+    uint64_t* empty = full + kTcStages;
+    uint64_t* accum = empty + kTcStages;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t m0 = blockIdx.x * kTcM;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kTcStages; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(accum, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 2) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(S::kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = *tmem_slot;
+    if (warp == 0 && lane == 0) {
+        for (uint32_t kb = 0; kb < kblocks; kb++) {
+            const uint32_t s = kb % kTcStages, round = kb / kTcStages;
+            if (!mbar_wait(&empty[s], (round & 1u) ^ 1u, ep.err)) break;
+            mbar_expect_tx(&full[s], S::kStage);
+            tma_load_2d(smem + s * S::kStage, &tmA, (int)(kb * kTcBK), (int)m0, &full[s]);
+            tma_load_2d(smem + s * S::kStage + S::kA, &tmB, (int)(kb * kTcBK), 0, &full[s]);
+        }
+    } else if (warp == 1 && lane == 0) {
+        bool ok = true;
+        for (uint32_t kb = 0; kb < kblocks; kb++) {
+            const uint32_t s = kb % kTcStages, round = kb / kTcStages;
+            if (!mbar_wait(&full[s], round & 1u, ep.err)) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint64_t a0 = sw128_desc(smem_u32(smem + s * S::kStage));
+            const uint64_t b0 = sw128_desc(smem_u32(smem + s * S::kStage + S::kA));
+#pragma unroll
+            for (int k = 0; k < kTcBK / 16; k++) {
+                const uint32_t acc = (kb | (uint32_t)k) ? 1u : 0u;
+                asm volatile(
+                    "{ .reg .pred p; setp.ne.b32 p, %4, 0; tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(
+                        taddr),
+                    "l"(a0 + (uint64_t)(2 * k)), "l"(b0 + (uint64_t)(2 * k)), "r"(S::kIdesc), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_u32(&empty[s]))
+                         : "memory");
+        }
+        if (ok)
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_u32(accum))
+                         : "memory");
+    } else if (warp >= 4) {
+        const int wq = warp - 4;
+        if (mbar_wait(accum, 0, ep.err)) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t row = m0 + (uint32_t)(wq * 32 + lane);
+            const bool live = row < ep.n;
+            const float sc = (live && ep.scale) ? ep.scale[row] : 1.0f;
+            float4 rh = make_float4(0, 0, 0, 0);
+            if (live && ep.mode == 1) rh = ep.rho[row];
+#pragma unroll 1
+            for (int c0 = 0; c0 < NR; c0 += 32) {
+                uint32_t v[32];
+                const uint32_t ta = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)c0;
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                      "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                    : "r"(ta));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (!live) continue;
+#pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    const uint32_t c = (uint32_t)(c0 + j);
+                    if (c >= ep.R) break;
+                    float y = sc * __uint_as_float(v[j]);
+                    if (ep.mode == 1) {
+                        const int ch = (int)(c % 3);
+                        const float rr = ch == 0 ? rh.x : (ch == 1 ? rh.y : rh.z);
+                        y = ep.resid[(size_t)c * ep.n + row] + rr * y;
+                    }
+                    ep.out[(size_t)c * ep.n + row] = y;
+                    if (ep.out16) ep.out16[(size_t)c * ep.ld16 + row] = __float2bfloat16_rn(y);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 2) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(S::kCols) : "memory");
+    }
+}
+
+// Host side: tensor maps through the driver entry point (no libcuda link needed).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+// 2-D bf16 tensor map over rows x cols (row length ld elements, ld % 64 == 0), box box_rows x 64.
+static bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t ld, uint32_t box_rows) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn || (ld % 64) != 0 || (reinterpret_cast<uintptr_t>(base) & 15u) != 0) return false;
+    const cuuint64_t dims[2] = {ld, rows};
+    const cuuint64_t strides[1] = {ld * 2};
+    const cuuint32_t box[2] = {64, box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int NR>
+static int launch_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv_bfloat16* Bt, const TcEpilogue& ep,
+                     cudaStream_t s) {
+    using S = TcShape<NR>;
+    CUtensorMap ma, mb;
+    if (!make_map(&ma, A, n, ld, kTcM) || !make_map(&mb, Bt, NR, ld, NR)) return -1;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_gemm_tc<NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::kSmem) != cudaSuccess)
+            return -2;
+        attr = true;
+    }
+    const uint32_t kblocks = ld / kTcBK;
+    k_gemm_tc<NR><<<(n + kTcM - 1) / kTcM, 256, S::kSmem, s>>>(ma, mb, kblocks, ep);
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+// Bt must have Rpad = the template width rows (zero padded) and ld columns.
+int launch_gemm_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv_bfloat16* Bt, uint32_t Rpad,
+                   const TcEpilogue& ep, cudaStream_t s) {
+    switch (Rpad) {
+        case 16: return launch_tc<16>(A, n, ld, Bt, ep, s);
+        case 32: return launch_tc<32>(A, n, ld, Bt, ep, s);
+        case 64: return launch_tc<64>(A, n, ld, Bt, ep, s);
+        case 128: return launch_tc<128>(A, n, ld, Bt, ep, s);
+        case 192: return launch_tc<192>(A, n, ld, Bt, ep, s);
+        case 256: return launch_tc<256>(A, n, ld, Bt, ep, s);
+        default: return -4;
+    }
+}
+
+uint32_t gemm_tc_width(uint32_t R) {
+    if (R <= 16) return 16;
+    if (R <= 32) return 32;
+    if (R <= 64) return 64;
+    if (R <= 128) return 128;
+    if (R <= 192) return 192;
+    if (R <= 256) return 256;
+    return 0;
+}
+
+}  // namespace rad

@@ -7,6 +7,7 @@
 // graph once per context and replays it, checking the device stop flag every
 // 32 batches.  Every kernel reads the device stop flag first, so batches after
 // the stop rule fired are no-ops and the result equals the reference's early exit.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -59,6 +60,12 @@ struct rad_ctx {
     size_t rows_cap = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
+    // dense form factors (rad_dense_capture)
+    float* d_F32 = nullptr;
+    __nv_bfloat16* d_F16 = nullptr;
+    float* d_scale = nullptr;
+    uint32_t dense_ld = 0;
+    bool dense_ready = false;
 };
 
 #define RAD_CUDA(ctx, call)                                                                         \
@@ -371,6 +378,9 @@ int rad_destroy(rad_ctx* c) {
     dfree(c->d_state);
     dfree(c->d_aux);
     dfree(c->d_rows);
+    dfree(c->d_F32);
+    dfree(c->d_F16);
+    dfree(c->d_scale);
     if (c->h_flag) cudaFreeHost(c->h_flag);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -405,6 +415,10 @@ int rad_upload_scene(rad_ctx* c, const float* vertices, const int32_t* indices, 
     drop_graph(c);
     free_batch(c->shoot);
     free_batch(c->aux);
+    dfree(c->d_F32);
+    dfree(c->d_F16);
+    dfree(c->d_scale);
+    c->dense_ready = false;
     dfree(c->d_verts);
     dfree(c->d_color);
     dfree(c->d_rho);
@@ -743,6 +757,219 @@ int rad_autotune(rad_ctx* c, uint32_t flags, rad_tuning* out) {
         out->us_per_hemicube = 1000.0 * best / (double)sh.size();
     }
     return RAD_OK;
+}
+
+int rad_dense_capture(rad_ctx* c, uint32_t flags, double* device_ms) {
+    if (!c) return RAD_E_INVALID;
+    if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
+    const uint32_t n = c->n, ld = (n + 63u) & ~63u;
+    dfree(c->d_F32);
+    dfree(c->d_F16);
+    dfree(c->d_scale);
+    c->dense_ready = false;
+    c->dense_ld = ld;
+    RAD_CUDA(c, cudaMalloc(&c->d_F16, sizeof(__nv_bfloat16) * (size_t)n * ld));
+    RAD_CUDA(c, cudaMalloc(&c->d_scale, sizeof(float) * n));
+    if (flags & RAD_DENSE_FP32) RAD_CUDA(c, cudaMalloc(&c->d_F32, sizeof(float) * (size_t)n * ld));
+    const uint32_t chunk = 128;
+    std::vector<uint32_t> ids(chunk);
+    cudaEvent_t e0, e1;
+    RAD_CUDA(c, cudaEventCreate(&e0));
+    RAD_CUDA(c, cudaEventCreate(&e1));
+    RAD_CUDA(c, cudaEventRecord(e0, c->stream));
+    for (uint32_t first = 0; first < n; first += chunk) {
+        const uint32_t cnt = std::min(chunk, n - first);
+        for (uint32_t k = 0; k < cnt; k++) ids[k] = first + k;
+        int rc = run_aux(c, ids.data(), cnt, false, true);
+        if (rc) return rc;
+        launch_dense_rows(c->aux.b.Fq, cnt, n, ld, first, c->d_F32, c->d_F16, c->d_scale, c->stream);
+        RAD_CUDA(c, cudaGetLastError());
+    }
+    RAD_CUDA(c, cudaEventRecord(e1, c->stream));
+    RAD_CUDA(c, cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (device_ms) *device_ms = ms;
+    c->dense_ready = true;
+    return RAD_OK;
+}
+
+int rad_dense_rows(rad_ctx* c, uint32_t first, uint32_t count, float* f32, uint16_t* bf16, float* scale) {
+    if (!c) return RAD_E_INVALID;
+    if (!c->dense_ready) return fail(c, RAD_E_STATE, "no dense capture");
+    if ((uint64_t)first + count > c->n) return fail(c, RAD_E_INVALID, "rows out of range");
+    const size_t n = c->n, ld = c->dense_ld;
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (f32) {
+        if (!c->d_F32) return fail(c, RAD_E_STATE, "FP32 rows were not kept");
+        RAD_CUDA(c, cudaMemcpy2D(f32, n * 4, c->d_F32 + (size_t)first * ld, ld * 4, n * 4, count, cudaMemcpyDeviceToHost));
+    }
+    if (bf16)
+        RAD_CUDA(c, cudaMemcpy2D(bf16, n * 2, c->d_F16 + (size_t)first * ld, ld * 2, n * 2, count, cudaMemcpyDeviceToHost));
+    if (scale) RAD_CUDA(c, cudaMemcpy(scale, c->d_scale + first, 4 * (size_t)count, cudaMemcpyDeviceToHost));
+    return RAD_OK;
+}
+
+int rad_gather_solve(rad_ctx* c, const float* emission, uint32_t R, const float* guess, double tol, uint32_t max_outer,
+                     uint32_t sweeps, float* radiosity, rad_gather_stats* stats) {
+    if (!c || !emission || !radiosity || R == 0) return RAD_E_INVALID;
+    if (!c->dense_ready || !c->d_F32) return fail(c, RAD_E_STATE, "needs rad_dense_capture with RAD_DENSE_FP32");
+    if (c->cfg.mode != RAD_MODE_PHYS) return fail(c, RAD_E_STATE, "the gathering solve needs PHYS reflectance");
+    const uint32_t Rpad = gemm_tc_width(R);
+    if (!Rpad) return fail(c, RAD_E_INVALID, "at most 256 right-hand sides");
+    const uint32_t n = c->n, ld = c->dense_ld;
+    const size_t nr = (size_t)n * R;
+    cudaStream_t s = c->stream;
+    float *dE = nullptr, *dB = nullptr, *dr = nullptr, *dd = nullptr;
+    __nv_bfloat16* d16[2] = {nullptr, nullptr};
+    double* dnrm = nullptr;
+    uint32_t* derr = nullptr;
+    int rc = RAD_OK;
+    auto cleanup = [&]() {
+        cudaFree(dE); cudaFree(dB); cudaFree(dr); cudaFree(dd);
+        cudaFree(d16[0]); cudaFree(d16[1]); cudaFree(dnrm); cudaFree(derr);
+    };
+#define G_CUDA(call)                                                                                  \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) {                                                                      \
+            c->err = std::string(#call) + ": " + cudaGetErrorString(e_);                              \
+            cleanup();                                                                                \
+            return e_ == cudaErrorMemoryAllocation ? RAD_E_NOMEM : RAD_E_CUDA;                        \
+        }                                                                                             \
+    } while (0)
+    G_CUDA(cudaMalloc(&dE, 4 * nr));
+    G_CUDA(cudaMalloc(&dB, 4 * nr));
+    G_CUDA(cudaMalloc(&dr, 4 * nr));
+    G_CUDA(cudaMalloc(&dd, 4 * nr));
+    G_CUDA(cudaMalloc(&d16[0], 2 * (size_t)Rpad * ld));
+    G_CUDA(cudaMalloc(&d16[1], 2 * (size_t)Rpad * ld));
+    G_CUDA(cudaMalloc(&dnrm, 8 * (size_t)R));
+    G_CUDA(cudaMalloc(&derr, 4));
+    G_CUDA(cudaMemsetAsync(derr, 0, 4, s));
+    G_CUDA(cudaMemcpyAsync(dE, emission, 4 * nr, cudaMemcpyHostToDevice, s));
+    G_CUDA(cudaMemcpyAsync(dB, guess ? guess : emission, 4 * nr, cudaMemcpyHostToDevice, s));
+    std::vector<double> enorm(R, 0.0), nrm(R);
+    for (uint32_t col = 0; col < R; col++) {
+        double a = 0;
+        for (uint32_t i = 0; i < n; i++) a += (double)emission[(size_t)col * n + i] * emission[(size_t)col * n + i];
+        enorm[col] = std::sqrt(a);
+    }
+    cudaEvent_t ev[4];
+    for (auto& e : ev) G_CUDA(cudaEventCreate(&e));
+    G_CUDA(cudaEventRecord(ev[0], s));
+    rad_gather_stats st{};
+    double sweep_ms = 0, resid_ms = 0;
+    for (uint32_t outer = 0;; outer++) {
+        G_CUDA(cudaMemsetAsync(dnrm, 0, 8 * (size_t)R, s));
+        G_CUDA(cudaEventRecord(ev[2], s));
+        launch_sgemm_resid(c->d_F32, n, ld, dB, dE, c->d_rho, R, dr, dnrm, s);
+        G_CUDA(cudaEventRecord(ev[3], s));
+        G_CUDA(cudaGetLastError());
+        G_CUDA(cudaMemcpyAsync(nrm.data(), dnrm, 8 * (size_t)R, cudaMemcpyDeviceToHost, s));
+        G_CUDA(cudaStreamSynchronize(s));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ev[2], ev[3]);
+        resid_ms += ms;
+        double res = 0;
+        for (uint32_t col = 0; col < R; col++)
+            if (enorm[col] > 0) res = std::max(res, std::sqrt(nrm[col]) / enorm[col]);
+        st.outer = outer + 1;
+        if (outer == 0) st.initial_residual = res;
+        st.residual = res;
+        if (res <= tol || outer >= max_outer) break;
+        // correction: d = r + rho o (F16 d), d0 = r
+        if (sweeps == 0) {
+            G_CUDA(cudaMemcpyAsync(dd, dr, 4 * nr, cudaMemcpyDeviceToDevice, s));
+        } else {
+            launch_pack_bf16(dr, n, R, ld, d16[0], Rpad, s);
+            G_CUDA(cudaEventRecord(ev[2], s));
+            int cur = 0;
+            for (uint32_t k = 0; k < sweeps; k++) {
+                TcEpilogue ep{};
+                ep.mode = 1;
+                ep.n = n;
+                ep.R = R;
+                ep.scale = c->d_scale;
+                ep.rho = c->d_rho;
+                ep.resid = dr;
+                ep.out = dd;
+                ep.out16 = d16[cur ^ 1];
+                ep.ld16 = ld;
+                ep.err = derr;
+                if (launch_gemm_tc(c->d_F16, n, ld, d16[cur], Rpad, ep, s) != 0) {
+                    cleanup();
+                    return fail(c, RAD_E_CUDA, "tcgen05 GEMM launch failed");
+                }
+                cur ^= 1;
+                st.sweeps++;
+            }
+            G_CUDA(cudaEventRecord(ev[3], s));
+            G_CUDA(cudaEventSynchronize(ev[3]));
+            ms = 0;
+            cudaEventElapsedTime(&ms, ev[2], ev[3]);
+            sweep_ms += ms;
+        }
+        launch_axpy(dB, dd, nr, s);
+        G_CUDA(cudaGetLastError());
+    }
+    G_CUDA(cudaEventRecord(ev[1], s));
+    G_CUDA(cudaEventSynchronize(ev[1]));
+    float total = 0;
+    cudaEventElapsedTime(&total, ev[0], ev[1]);
+    for (auto& e : ev) cudaEventDestroy(e);
+    uint32_t herr = 0;
+    G_CUDA(cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost));
+    G_CUDA(cudaMemcpy(radiosity, dB, 4 * nr, cudaMemcpyDeviceToHost));
+#undef G_CUDA
+    cleanup();
+    st.device_ms = total;
+    st.sweep_ms = sweep_ms;
+    st.resid_ms = resid_ms;
+    if (stats) *stats = st;
+    if (herr) rc = fail(c, RAD_E_TIMEOUT, "a tcgen05 pipeline wait timed out");
+    return rc;
+}
+
+int rad_bf16_gemm(int device, const uint16_t* A, const uint16_t* Bt, uint32_t n, uint32_t k, uint32_t R, float* C) {
+    if (!A || !Bt || !C || n == 0 || k == 0 || R == 0) return RAD_E_INVALID;
+    const uint32_t Rpad = gemm_tc_width(R);
+    if (!Rpad) return RAD_E_INVALID;
+    if (cudaSetDevice(device) != cudaSuccess) return RAD_E_CUDA;
+    const uint32_t ld = (k + 63u) & ~63u;
+    __nv_bfloat16 *dA = nullptr, *dB = nullptr;
+    float* dC = nullptr;
+    uint32_t* derr = nullptr;
+    int rc = RAD_OK;
+    if (cudaMalloc(&dA, 2 * (size_t)n * ld) != cudaSuccess || cudaMalloc(&dB, 2 * (size_t)Rpad * ld) != cudaSuccess ||
+        cudaMalloc(&dC, 4 * (size_t)n * R) != cudaSuccess || cudaMalloc(&derr, 4) != cudaSuccess)
+        rc = RAD_E_NOMEM;
+    if (!rc) {
+        cudaMemset(dA, 0, 2 * (size_t)n * ld);
+        cudaMemset(dB, 0, 2 * (size_t)Rpad * ld);
+        cudaMemset(derr, 0, 4);
+        cudaMemcpy2D(dA, 2 * ld, A, 2 * (size_t)k, 2 * (size_t)k, n, cudaMemcpyHostToDevice);
+        cudaMemcpy2D(dB, 2 * ld, Bt, 2 * (size_t)k, 2 * (size_t)k, R, cudaMemcpyHostToDevice);
+        TcEpilogue ep{};
+        ep.mode = 0;
+        ep.n = n;
+        ep.R = R;
+        ep.out = dC;
+        ep.err = derr;
+        if (launch_gemm_tc(dA, n, ld, dB, Rpad, ep, 0) != 0) rc = RAD_E_CUDA;
+        if (!rc && cudaDeviceSynchronize() != cudaSuccess) rc = RAD_E_CUDA;
+        uint32_t herr = 0;
+        if (!rc) cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost);
+        if (!rc && herr) rc = RAD_E_TIMEOUT;
+        if (!rc) cudaMemcpy(C, dC, 4 * (size_t)n * R, cudaMemcpyDeviceToHost);
+    }
+    cudaFree(dA);
+    cudaFree(dB);
+    cudaFree(dC);
+    cudaFree(derr);
+    return rc;
 }
 
 int rad_raster_counters(rad_ctx* c, uint64_t* out) {

@@ -118,6 +118,32 @@ void launch_update(const Geo& g, const Batch& b, const float4* color, const floa
 void launch_emitters(const Geo& g, const Batch& b, float4* rad, float4* illum, const float* area,
                      double tol, double* partials, DevState* st, cudaStream_t s);
 void launch_areas(const float* verts, uint32_t n, float* area, cudaStream_t s);
+
+// dense.cu
+}  // namespace rad
+#include <cuda_bf16.h>
+namespace rad {
+struct TcEpilogue {
+    int mode;                  // 0: out = scale*acc ; 1: out = resid + rho o (scale*acc)
+    uint32_t n, R;             // rows, output columns
+    const float* scale;        // n (may be null: 1)
+    const float4* rho;         // n (mode 1)
+    const float* resid;        // R x n column-major (mode 1)
+    float* out;                // R x n column-major
+    __nv_bfloat16* out16;      // R x ld16 (next operand), may be null
+    uint32_t ld16;
+    uint32_t* err;
+};
+void launch_dense_rows(const unsigned long long* Fq, uint32_t count, uint32_t n, uint32_t ld, uint32_t first,
+                       float* F32, __nv_bfloat16* F16, float* scale, cudaStream_t s);
+void launch_sgemm_resid(const float* F, uint32_t n, uint32_t ld, const float* X, const float* E, const float4* rho,
+                        uint32_t R, float* r, double* nrm, cudaStream_t s);
+void launch_pack_bf16(const float* X, uint32_t n, uint32_t R, uint32_t ld, __nv_bfloat16* Xt, uint32_t Rpad,
+                      cudaStream_t s);
+void launch_axpy(float* y, const float* x, size_t total, cudaStream_t s);
+int launch_gemm_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv_bfloat16* Bt, uint32_t Rpad,
+                   const TcEpilogue& ep, cudaStream_t s);
+uint32_t gemm_tc_width(uint32_t R);
 void launch_fftab(uint32_t W, float* fftab, cudaStream_t s);
 
 }  // namespace rad

@@ -1,0 +1,81 @@
+"""Precision form: tcgen05 BF16 GEMM, dense form-factor capture, gathering solve.
+
+Bars: the tcgen05 GEMM equals an FP64 product of the same BF16 inputs to FP32
+accumulation accuracy (1e-5 of sum |a||b|); captured FP32 rows are bit-identical
+to the hemicube pipeline's rows and BF16 rows are within one BF16 rounding
+(2^-8 relative to the row scale); the gathering solve reaches its tolerance and
+agrees with an FP64 dense solve on the same FP32 rows to 1e-5 relative.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _bf16_bits(x):
+    u = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)  # round to nearest even
+    return r
+
+
+def _bf16_val(bits):
+    return (bits.astype(np.uint32) << 16).view(np.float32)
+
+
+@pytest.mark.parametrize("n,k,R", [(128, 64, 16), (200, 130, 3), (300, 257, 40), (513, 1000, 192), (256, 640, 256)])
+def test_bf16_gemm_tcgen05(lib, n, k, R):
+    rng = np.random.default_rng(n + k + R)
+    A = _bf16_bits(rng.uniform(-1, 1, (n, k)).astype(np.float32))
+    B = _bf16_bits(rng.uniform(-1, 1, (R, k)).astype(np.float32))
+    C = lib.bf16_gemm(A, B)
+    a = _bf16_val(A).astype(np.float64)
+    b = _bf16_val(B).astype(np.float64)
+    ref = (a @ b.T).T
+    bound = (np.abs(a) @ np.abs(b).T).T
+    assert np.all(np.abs(C - ref) <= 1e-5 * bound + 1e-30)
+
+
+@pytest.fixture(scope="module")
+def box(lib):
+    from radiosity_gb300 import scenes
+
+    return scenes.room_with_boxes(target=1500, seed=21)
+
+
+def _solver(lib, sc, W=64, K=16):
+    s = lib.Solver(hemicube_side=W, hemicubes_count=K, mode=1)
+    s.upload(sc["vertices"], sc["color"], sc["radiosity"], sc["illumination"], reflectance=sc["reflectance"])
+    return s
+
+
+def test_dense_capture_rows(lib, box):
+    with _solver(lib, box) as s:
+        s.dense_capture(keep_fp32=True)
+        f32, bits, scale = s.dense_rows(0, box["n"])
+        sh = np.array([0, 7, box["n"] // 2, box["n"] - 1], np.uint32)
+        rows = s.ff_rows(sh)
+    assert np.array_equal(f32[sh].view(np.uint32), rows.view(np.uint32))
+    mx = f32.max(axis=1)
+    assert np.allclose(scale[mx > 0], mx[mx > 0])
+    approx = _bf16_val(bits) * scale[:, None]
+    assert np.all(np.abs(approx - f32) <= 2.0 ** -8 * scale[:, None] + 1e-30)
+
+
+def test_gather_solve_matches_fp64(lib, box):
+    n = box["n"]
+    rng = np.random.default_rng(3)
+    E = np.zeros((6, n), np.float32)
+    for v in range(2):  # two emission vectors x RGB
+        em = rng.choice(n, 3, replace=False)
+        E[3 * v:3 * v + 3, em] = rng.uniform(1, 20, (3, 3)).astype(np.float32)
+    with _solver(lib, box) as s:
+        s.dense_capture(keep_fp32=True)
+        F, _, _ = s.dense_rows(0, n)
+        B, st = s.gather(E, tol=1e-6, max_outer=60, sweeps=6)
+    assert st.residual <= 1e-6 and st.sweeps > 0
+    rho = box["reflectance"].reshape(n, 3).astype(np.float64)
+    F64 = F.astype(np.float64)
+    for c in range(6):
+        A = np.eye(n) - rho[:, c % 3][:, None] * F64
+        ref = np.linalg.solve(A, E[c].astype(np.float64))
+        assert np.linalg.norm(B[c] - ref) <= 1e-5 * np.linalg.norm(ref)
