@@ -176,9 +176,33 @@ typedef struct rad_gather_stats {
 int rad_gather_solve(rad_ctx* ctx, const float* emission, uint32_t R, const float* guess, double tol,
                      uint32_t max_outer, uint32_t sweeps, float* radiosity, rad_gather_stats* stats);
 
+/* r = E + rho o (F B) - B with the FP32 rows (column-major N x R host arrays); with B = E
+ * this is the first-shot direct light rho o (F E). */
+int rad_gather_residual(rad_ctx* ctx, const float* emission, uint32_t R, const float* radiosity, float* residual);
+
 /* Diagnostic: C = A * Bt^T on the tcgen05 path (A n x k, Bt R x k BF16 bits, row-major;
  * C column-major R x n FP32), on `device`. */
 int rad_bf16_gemm(int device, const uint16_t* A, const uint16_t* Bt, uint32_t n, uint32_t k, uint32_t R, float* C);
+
+/* ---- Learned warm start -------------------------------------------------------------
+ * No counterpart in the reference.  A per-patch MLP, 32 -> 128 -> 128 -> 128 -> 128 -> 3
+ * with ReLU, BF16 weights (FP32 master copy, Adam) and FP32 accumulation, trained and
+ * evaluated by this library's own kernels.  Its prediction only seeds rad_gather_solve,
+ * which still iterates to the same tolerance.  Rows of X are 32 features per patch, rows
+ * of T / Y are 3 outputs; host arrays, row-major. */
+typedef struct rad_mlp rad_mlp;
+int rad_mlp_create(int device, uint64_t seed, rad_mlp** out);
+int rad_mlp_destroy(rad_mlp* mlp);
+uint32_t rad_mlp_param_count(void);
+/* FP32 master parameters: per layer W[out][in] then b[out]. */
+int rad_mlp_get_params(rad_mlp* mlp, float* params);
+int rad_mlp_set_params(rad_mlp* mlp, const float* params);
+int rad_mlp_predict(rad_mlp* mlp, const float* X, uint32_t P, float* Y);
+/* Mean-squared-error loss of (X, T) and its gradient w.r.t. every parameter (no update). */
+int rad_mlp_gradients(rad_mlp* mlp, const float* X, const float* T, uint32_t P, float* grads, double* loss);
+/* Adam epochs over (X, T) in consecutive batches; the data set is copied to the device once. */
+int rad_mlp_train(rad_mlp* mlp, const float* X, const float* T, uint32_t P, uint32_t epochs, uint32_t batch,
+                  float lr, double* final_loss, double* device_ms);
 
 /* Raster counters of the last rad_profile_stages call (8 values): triangle-bin pairs,
  * small triangles (one lane each), their bbox pixels, large triangles (one warp each),

@@ -33,7 +33,9 @@ EXPORTS = [
     "rad_set_state", "rad_download", "rad_ff_table", "rad_select_shooters", "rad_render_item_buffers",
     "rad_reduce_item_buffers", "rad_ff_rows", "rad_shoot", "rad_profile_stages", "rad_scene_reference",
     "rad_reduce_items_noalloc", "rad_raster_counters", "rad_autotune", "rad_dense_capture",
-    "rad_dense_rows", "rad_gather_solve", "rad_bf16_gemm", "rad_strerror", "rad_last_error",
+    "rad_dense_rows", "rad_gather_solve", "rad_gather_residual", "rad_bf16_gemm", "rad_mlp_create", "rad_mlp_destroy",
+    "rad_mlp_param_count", "rad_mlp_get_params", "rad_mlp_set_params", "rad_mlp_predict", "rad_mlp_gradients",
+    "rad_mlp_train", "rad_strerror", "rad_last_error",
 ]
 STAGES = ["select", "camera", "setup", "bins", "raster", "update", "emitters"]
 STAGE_KERNELS = [1, 1, 1, 2, 1, 1, 1]
@@ -128,7 +130,17 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rad_dense_rows.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, vp, vp, vp]
     L.rad_gather_solve.argtypes = [vp, _f32p, ctypes.c_uint32, vp, ctypes.c_double, ctypes.c_uint32,
                                    ctypes.c_uint32, _f32p, P(RadGatherStats)]
+    L.rad_gather_residual.argtypes = [vp, _f32p, ctypes.c_uint32, _f32p, _f32p]
     L.rad_bf16_gemm.argtypes = [ctypes.c_int, vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _f32p]
+    L.rad_mlp_create.argtypes = [ctypes.c_int, ctypes.c_uint64, P(vp)]
+    L.rad_mlp_destroy.argtypes = [vp]
+    L.rad_mlp_param_count.argtypes = []
+    L.rad_mlp_get_params.argtypes = [vp, _f32p]
+    L.rad_mlp_set_params.argtypes = [vp, _f32p]
+    L.rad_mlp_predict.argtypes = [vp, _f32p, ctypes.c_uint32, _f32p]
+    L.rad_mlp_gradients.argtypes = [vp, _f32p, _f32p, ctypes.c_uint32, _f32p, P(ctypes.c_double)]
+    L.rad_mlp_train.argtypes = [vp, _f32p, _f32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
+                                P(ctypes.c_double), P(ctypes.c_double)]
     L.rad_autotune.argtypes = [vp, ctypes.c_uint32, P(RadTuning)]
     L.rad_raster_counters.argtypes = [vp, np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")]
     L.rad_reduce_items_noalloc.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp, vp]
@@ -140,6 +152,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     for name in EXPORTS:
         getattr(L, name).restype = getattr(L, name).restype if name in ("rad_strerror", "rad_last_error") \
             else ctypes.c_int
+    L.rad_mlp_param_count.restype = ctypes.c_uint32
     _LIB = L
     return L
 
@@ -335,6 +348,15 @@ class Solver:
                                             out.reshape(-1), ctypes.byref(st)), "rad_gather_solve")
         return out, st
 
+    def gather_residual(self, emission, radiosity):
+        """rad_gather_residual: r = E + rho o (F B) - B (R x N arrays)."""
+        E = np.ascontiguousarray(emission, np.float32)
+        B = np.ascontiguousarray(radiosity, np.float32)
+        r = np.zeros_like(E)
+        self._check(self.L.rad_gather_residual(self.h, E.reshape(-1), E.shape[0], B.reshape(-1), r.reshape(-1)),
+                    "rad_gather_residual")
+        return r
+
     RASTER_COUNTERS = ["pairs", "small_tris", "small_px", "big_tris", "big_stamps", "stamps_visited",
                        "stamps_inside", "big_px_written"]
 
@@ -347,3 +369,70 @@ class Solver:
         st = RadStats()
         self._check(self.L.rad_shoot(self.h, n_shots, ctypes.byref(st)), "rad_shoot")
         return st
+
+
+class MLP:
+    """rad_mlp: the per-patch warm-start network (BF16 weights, FP32 accumulation)."""
+
+    IN, HID, OUT = 32, 128, 3
+    DIMS = [32, 128, 128, 128, 128, 3]
+
+    def __init__(self, seed: int = 0, device: int = 0):
+        self.L = load()
+        h = ctypes.c_void_p()
+        rc = self.L.rad_mlp_create(device, seed, ctypes.byref(h))
+        if rc:
+            raise RadError(rc, "rad_mlp_create")
+        self.h = h
+        self.nparams = int(self.L.rad_mlp_param_count())
+
+    def close(self):
+        if self.h:
+            self.L.rad_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.nparams, np.float32)
+        rc = self.L.rad_mlp_get_params(self.h, out)
+        if rc:
+            raise RadError(rc, "rad_mlp_get_params")
+        return out
+
+    def set_params(self, p):
+        rc = self.L.rad_mlp_set_params(self.h, np.ascontiguousarray(p, np.float32))
+        if rc:
+            raise RadError(rc, "rad_mlp_set_params")
+
+    def predict(self, X) -> np.ndarray:
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.zeros((X.shape[0], 3), np.float32)
+        rc = self.L.rad_mlp_predict(self.h, X.reshape(-1), X.shape[0], Y.reshape(-1))
+        if rc:
+            raise RadError(rc, "rad_mlp_predict")
+        return Y
+
+    def gradients(self, X, T):
+        X = np.ascontiguousarray(X, np.float32)
+        T = np.ascontiguousarray(T, np.float32)
+        g = np.zeros(self.nparams, np.float32)
+        loss = ctypes.c_double()
+        rc = self.L.rad_mlp_gradients(self.h, X.reshape(-1), T.reshape(-1), X.shape[0], g, ctypes.byref(loss))
+        if rc:
+            raise RadError(rc, "rad_mlp_gradients")
+        return g, loss.value
+
+    def train(self, X, T, epochs: int, batch: int = 4096, lr: float = 1e-3):
+        X = np.ascontiguousarray(X, np.float32)
+        T = np.ascontiguousarray(T, np.float32)
+        loss, ms = ctypes.c_double(), ctypes.c_double()
+        rc = self.L.rad_mlp_train(self.h, X.reshape(-1), T.reshape(-1), X.shape[0], epochs, batch, lr,
+                                  ctypes.byref(loss), ctypes.byref(ms))
+        if rc:
+            raise RadError(rc, "rad_mlp_train")
+        return loss.value, ms.value

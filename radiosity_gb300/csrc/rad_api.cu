@@ -933,6 +933,29 @@ int rad_gather_solve(rad_ctx* c, const float* emission, uint32_t R, const float*
     return rc;
 }
 
+int rad_gather_residual(rad_ctx* c, const float* emission, uint32_t R, const float* radiosity, float* residual) {
+    if (!c || !emission || !radiosity || !residual || R == 0) return RAD_E_INVALID;
+    if (!c->dense_ready || !c->d_F32) return fail(c, RAD_E_STATE, "needs rad_dense_capture with RAD_DENSE_FP32");
+    const size_t nr = (size_t)c->n * R;
+    float *dE = nullptr, *dB = nullptr, *dr = nullptr;
+    int rc = RAD_OK;
+    if (cudaMalloc(&dE, 4 * nr) != cudaSuccess || cudaMalloc(&dB, 4 * nr) != cudaSuccess ||
+        cudaMalloc(&dr, 4 * nr) != cudaSuccess)
+        rc = fail(c, RAD_E_NOMEM, "residual buffers");
+    if (!rc) {
+        cudaMemcpyAsync(dE, emission, 4 * nr, cudaMemcpyHostToDevice, c->stream);
+        cudaMemcpyAsync(dB, radiosity, 4 * nr, cudaMemcpyHostToDevice, c->stream);
+        launch_sgemm_resid(c->d_F32, c->n, c->dense_ld, dB, dE, c->d_rho, R, dr, nullptr, c->stream);
+        cudaMemcpyAsync(residual, dr, 4 * nr, cudaMemcpyDeviceToHost, c->stream);
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(c->stream) != cudaSuccess)
+            rc = fail(c, RAD_E_CUDA, "residual GEMM failed");
+    }
+    cudaFree(dE);
+    cudaFree(dB);
+    cudaFree(dr);
+    return rc;
+}
+
 int rad_bf16_gemm(int device, const uint16_t* A, const uint16_t* Bt, uint32_t n, uint32_t k, uint32_t R, float* C) {
     if (!A || !Bt || !C || n == 0 || k == 0 || R == 0) return RAD_E_INVALID;
     const uint32_t Rpad = gemm_tc_width(R);

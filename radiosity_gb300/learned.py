@@ -1,0 +1,101 @@
+"""Learned warm start for the gathering solve: features, targets and the training loop.
+
+A per-patch MLP (``radiosity_gb300.MLP``, this library's own BF16 kernels) maps 32
+features of a patch to its converged radiosity.  Features, per scene:
+  0-2   patch centre, normalised to the scene bounding box
+  3-5   unit normal
+  6     area / mean area
+  7-9   RGB reflectance
+  10-12 log1p(first-shot direct light / s), s = per-channel mean direct light
+  13-15 log1p(emission / s)
+  16-31 sin / cos of 2*pi*(p . b_k) for 8 fixed random directions b_k (Fourier features)
+Target: log1p(max(B - E, 0) / s); the guess is B0 = E + s * expm1(max(y, 0)).
+The prediction only seeds rad_gather_solve, which still iterates to its tolerance.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _lib, scenes
+
+_FOURIER = np.random.default_rng(1234).normal(0.0, 2.0, (8, 3)).astype(np.float64)
+
+
+def patch_geometry(vertices: np.ndarray):
+    q = vertices.reshape(-1, 4, 3).astype(np.float64)
+    c = q.mean(1)
+    n = np.cross(q[:, 3] - q[:, 0], q[:, 1] - q[:, 0])
+    a = 0.5 * np.linalg.norm(np.cross(q[:, 0] - q[:, 2], q[:, 1] - q[:, 3]), axis=1)
+    n = n / np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-20)
+    return c, n, a
+
+
+def scale_of(direct: np.ndarray) -> np.ndarray:
+    """Per-channel normalisation s (3,) of a scene from its direct light (N x 3)."""
+    return direct.mean(0) + 1e-12
+
+
+def features(scene: dict, direct: np.ndarray) -> np.ndarray:
+    """32 features per patch; direct is N x 3."""
+    c, n, a = patch_geometry(scene["vertices"])
+    lo, hi = c.min(0), c.max(0)
+    p = (c - lo) / np.maximum(hi - lo, 1e-9)
+    s = scale_of(direct)
+    E = scene["radiosity"].reshape(-1, 3).astype(np.float64)
+    rho = scene["reflectance"].reshape(-1, 3).astype(np.float64)
+    ph = 2 * np.pi * p @ _FOURIER.T
+    X = np.concatenate([p, n, (a / a.mean())[:, None], rho, np.log1p(np.maximum(direct, 0) / s),
+                        np.log1p(E / s), np.sin(ph), np.cos(ph)], axis=1)
+    return X.astype(np.float32)
+
+
+def targets(scene: dict, B: np.ndarray, direct: np.ndarray) -> np.ndarray:
+    """B is N x 3 converged radiosity."""
+    E = scene["radiosity"].reshape(-1, 3).astype(np.float64)
+    return np.log1p(np.maximum(B - E, 0) / scale_of(direct)).astype(np.float32)
+
+
+def decode(scene: dict, direct: np.ndarray, Y: np.ndarray) -> np.ndarray:
+    E = scene["radiosity"].reshape(-1, 3).astype(np.float64)
+    return (E + scale_of(direct) * np.expm1(np.maximum(Y, 0))).astype(np.float32)
+
+
+def capture(scene: dict, W: int = 128) -> "_lib.Solver":
+    """A PHYS solver with the scene's dense form factors captured (FP32 + BF16)."""
+    s = _lib.Solver(hemicube_side=W, hemicubes_count=16, mode=_lib.MODE_PHYS)
+    s.upload(scene["vertices"], scene["color"], scene["radiosity"], scene["illumination"],
+             reflectance=scene["reflectance"])
+    s.dense_capture(keep_fp32=True)
+    return s
+
+
+def emission_block(scene: dict) -> np.ndarray:
+    """The scene's emission as a 3 x N column-major block (one RHS per channel)."""
+    return np.ascontiguousarray(scene["radiosity"].reshape(-1, 3).T, np.float32)
+
+
+def direct_light(solver: "_lib.Solver", E: np.ndarray) -> np.ndarray:
+    """First-shot direct light rho o (F E) as N x 3."""
+    return solver.gather_residual(E, E).T.astype(np.float64)
+
+
+def training_set(n_scenes: int, seed: int = 0, patches=(2000, 6000), W: int = 128, tol: float = 1e-6):
+    """Solver-generated (X, T) pairs from ``cornell_variant`` scenes."""
+    rng = np.random.default_rng(seed)
+    Xs, Ts = [], []
+    for k in range(n_scenes):
+        target = int(np.exp(rng.uniform(np.log(patches[0]), np.log(patches[1]))))
+        sc = scenes.cornell_variant(target, seed=int(rng.integers(1 << 30)))
+        with capture(sc, W) as s:
+            E = emission_block(sc)
+            B, _ = s.gather(E, tol=tol, max_outer=80, sweeps=8)
+            d = direct_light(s, E)
+        Xs.append(features(sc, d))
+        Ts.append(targets(sc, B.T.astype(np.float64), d))
+    return np.concatenate(Xs), np.concatenate(Ts)
+
+
+def warm_start(mlp: "_lib.MLP", scene: dict, direct: np.ndarray) -> np.ndarray:
+    """3 x N guess for rad_gather_solve."""
+    Y = mlp.predict(features(scene, direct))
+    return np.ascontiguousarray(decode(scene, direct, Y).T)

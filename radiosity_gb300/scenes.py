@@ -162,3 +162,36 @@ def _concat(a: dict, b: dict) -> dict:
         out[k] = np.concatenate([a[k], b[k]])
     out["n"] = a["n"] + b["n"]
     return out
+
+
+def cornell_variant(target: int = 5000, seed: int = 0) -> dict:
+    """A seeded variation of ``cornell_box`` for training data: box size, block sizes and
+    positions, wall reflectances, and the light's size, position and emission vary."""
+    rng = np.random.default_rng(seed)
+    S = float(rng.uniform(4.0, 7.0))
+    zero = (0.0, 0.0, 0.0)
+
+    def rho():
+        return tuple(rng.uniform(0.1, 0.8, 3))
+
+    parts = []
+    parts.append((_rect((0, 0, 0), (S, 0, 0), (0, 0, S), np.array([0, 1.0, 0])), rho(), zero, 0))
+    parts.append((_rect((0, S, 0), (S, 0, 0), (0, 0, S), np.array([0, -1.0, 0])), rho(), zero, 1))
+    parts.append((_rect((0, 0, S), (S, 0, 0), (0, S, 0), np.array([0, 0, -1.0])), rho(), zero, 2))
+    parts.append((_rect((0, 0, 0), (0, 0, S), (0, S, 0), np.array([1.0, 0, 0])), rho(), zero, 3))
+    parts.append((_rect((S, 0, 0), (0, 0, S), (0, S, 0), np.array([-1.0, 0, 0])), rho(), zero, 4))
+    for b in range(2):
+        w, h, d = rng.uniform(0.15, 0.35, 3) * S
+        h *= 1.0 + b
+        x0 = rng.uniform(0.05 * S, S - w - 0.05 * S)
+        z0 = rng.uniform(0.05 * S, S - d - 0.05 * S)
+        r = rho()
+        for f in _box_faces((x0, 0.0, z0), (x0 + w, min(h, 0.8 * S), z0 + d)):
+            parts.append((f, r, zero, 5 + b))
+    lw, ld = rng.uniform(0.15, 0.35, 2) * S
+    lx = rng.uniform(0.1 * S, S - lw - 0.1 * S)
+    lz = rng.uniform(0.1 * S, S - ld - 0.1 * S)
+    em = tuple(rng.uniform(5.0, 20.0, 3))
+    light = _rect((lx, S - 0.005, lz), (lw, 0, 0), (0, 0, ld), np.array([0, -1.0, 0]))
+    edge = _fit_edge(parts, target)
+    return _concat(_assemble(parts, edge), _assemble([(light, (0.8, 0.8, 0.8), em, 7)], edge))
