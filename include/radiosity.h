@@ -204,6 +204,21 @@ int rad_mlp_gradients(rad_mlp* mlp, const float* X, const float* T, uint32_t P, 
 int rad_mlp_train(rad_mlp* mlp, const float* X, const float* T, uint32_t P, uint32_t epochs, uint32_t batch,
                   float lr, double* final_loss, double* device_ms);
 
+/* ---- Many scenes under one CUDA graph ---------------------------------------------------
+ * One graph replay advances every context by one shoot batch; the contexts' batches are
+ * parallel branches of the graph, so scenes of uneven size share the GPU.  Contexts must
+ * be on one device, have a scene uploaded, and must not be used elsewhere while the multi
+ * object exists.  No counterpart in the reference (one scene per process). */
+typedef struct rad_multi rad_multi;
+int rad_multi_create(rad_ctx* const* ctxs, uint32_t count, rad_multi** out);
+/* Replays up to n_replays times, stopping once every context's stop rule fired.
+ * stop_replay[i] = replay index (1-based) after which context i had stopped, 0 if it never
+ * did; stop_ms[i] = device time from the start of the call to the end of that replay
+ * (may be NULL); *replays and *device_ms receive the totals. */
+int rad_multi_shoot(rad_multi* m, uint32_t n_replays, uint32_t* stop_replay, double* stop_ms, uint32_t* replays,
+                    double* device_ms);
+int rad_multi_destroy(rad_multi* m);
+
 /* Raster counters of the last rad_profile_stages call (8 values): triangle-bin pairs,
  * small triangles (one lane each), their bbox pixels, large triangles (one warp each),
  * their 8x4 stamps, stamps visited, stamps wholly inside, large-triangle pixels written. */

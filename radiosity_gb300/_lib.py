@@ -35,7 +35,7 @@ EXPORTS = [
     "rad_reduce_items_noalloc", "rad_raster_counters", "rad_autotune", "rad_dense_capture",
     "rad_dense_rows", "rad_gather_solve", "rad_gather_residual", "rad_bf16_gemm", "rad_mlp_create", "rad_mlp_destroy",
     "rad_mlp_param_count", "rad_mlp_get_params", "rad_mlp_set_params", "rad_mlp_predict", "rad_mlp_gradients",
-    "rad_mlp_train", "rad_strerror", "rad_last_error",
+    "rad_mlp_train", "rad_multi_create", "rad_multi_shoot", "rad_multi_destroy", "rad_strerror", "rad_last_error",
 ]
 STAGES = ["select", "camera", "setup", "bins", "raster", "update", "emitters"]
 STAGE_KERNELS = [1, 1, 1, 2, 1, 1, 1]
@@ -141,6 +141,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rad_mlp_gradients.argtypes = [vp, _f32p, _f32p, ctypes.c_uint32, _f32p, P(ctypes.c_double)]
     L.rad_mlp_train.argtypes = [vp, _f32p, _f32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
                                 P(ctypes.c_double), P(ctypes.c_double)]
+    L.rad_multi_create.argtypes = [P(vp), ctypes.c_uint32, P(vp)]
+    L.rad_multi_shoot.argtypes = [vp, ctypes.c_uint32, vp, vp, P(ctypes.c_uint32), P(ctypes.c_double)]
+    L.rad_multi_destroy.argtypes = [vp]
     L.rad_autotune.argtypes = [vp, ctypes.c_uint32, P(RadTuning)]
     L.rad_raster_counters.argtypes = [vp, np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")]
     L.rad_reduce_items_noalloc.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp, vp]
@@ -436,3 +439,40 @@ class MLP:
         if rc:
             raise RadError(rc, "rad_mlp_train")
         return loss.value, ms.value
+
+
+class Multi:
+    """rad_multi: many solvers advanced together, one CUDA graph replay per batch."""
+
+    def __init__(self, solvers):
+        self.L = load()
+        self.solvers = list(solvers)
+        arr = (ctypes.c_void_p * len(self.solvers))(*[s.h.value for s in self.solvers])
+        h = ctypes.c_void_p()
+        rc = self.L.rad_multi_create(arr, len(self.solvers), ctypes.byref(h))
+        if rc:
+            raise RadError(rc, "rad_multi_create")
+        self.h = h
+
+    def shoot(self, n_replays: int):
+        n = len(self.solvers)
+        at = np.zeros(n, np.uint32)
+        ms = np.zeros(n, np.float64)
+        reps = ctypes.c_uint32()
+        total = ctypes.c_double()
+        rc = self.L.rad_multi_shoot(self.h, n_replays, at.ctypes.data_as(ctypes.c_void_p),
+                                    ms.ctypes.data_as(ctypes.c_void_p), ctypes.byref(reps), ctypes.byref(total))
+        if rc:
+            raise RadError(rc, "rad_multi_shoot")
+        return at, ms, reps.value, total.value
+
+    def close(self):
+        if self.h:
+            self.L.rad_multi_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

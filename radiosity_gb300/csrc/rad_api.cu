@@ -995,6 +995,127 @@ int rad_bf16_gemm(int device, const uint16_t* A, const uint16_t* Bt, uint32_t n,
     return rc;
 }
 
+namespace {
+__global__ void k_gather_flags(DevState* const* states, uint32_t count, uint32_t* out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+        out[i] = states[i]->stopped;
+}
+}  // namespace
+
+struct rad_multi {
+    std::vector<rad_ctx*> ctxs;
+    cudaStream_t stream = nullptr;
+    std::vector<cudaEvent_t> fork, join;
+    DevState** d_states = nullptr;
+    uint32_t* d_flags = nullptr;
+    uint32_t* h_flags = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+};
+
+int rad_multi_destroy(rad_multi* m) {
+    if (!m) return RAD_E_INVALID;
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    if (m->exec) cudaGraphExecDestroy(m->exec);
+    if (m->graph) cudaGraphDestroy(m->graph);
+    for (auto e : m->fork) cudaEventDestroy(e);
+    for (auto e : m->join) cudaEventDestroy(e);
+    if (m->t0) cudaEventDestroy(m->t0);
+    if (m->t1) cudaEventDestroy(m->t1);
+    cudaFree(m->d_states);
+    cudaFree(m->d_flags);
+    if (m->h_flags) cudaFreeHost(m->h_flags);
+    if (m->stream) cudaStreamDestroy(m->stream);
+    delete m;
+    return RAD_OK;
+}
+
+int rad_multi_create(rad_ctx* const* ctxs, uint32_t count, rad_multi** out) {
+    if (!ctxs || count == 0 || !out) return RAD_E_INVALID;
+    *out = nullptr;
+    const int dev = ctxs[0]->cfg.device;
+    for (uint32_t i = 0; i < count; i++)
+        if (!ctxs[i] || !ctxs[i]->n || ctxs[i]->cfg.device != dev) return RAD_E_INVALID;
+    if (cudaSetDevice(dev) != cudaSuccess) return RAD_E_CUDA;
+    rad_multi* m = new rad_multi();
+    m->ctxs.assign(ctxs, ctxs + count);
+    auto bail = [&](int code) {
+        rad_multi_destroy(m);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(RAD_E_CUDA);
+    if (cudaEventCreate(&m->t0) != cudaSuccess || cudaEventCreate(&m->t1) != cudaSuccess) return bail(RAD_E_CUDA);
+    m->fork.resize(count);
+    m->join.resize(count);
+    for (uint32_t i = 0; i < count; i++) {
+        if (cudaEventCreateWithFlags(&m->fork[i], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&m->join[i], cudaEventDisableTiming) != cudaSuccess)
+            return bail(RAD_E_CUDA);
+        cudaStreamSynchronize(ctxs[i]->stream);
+    }
+    std::vector<DevState*> st(count);
+    for (uint32_t i = 0; i < count; i++) st[i] = ctxs[i]->d_state;
+    if (cudaMalloc(&m->d_states, sizeof(DevState*) * count) != cudaSuccess ||
+        cudaMalloc(&m->d_flags, sizeof(uint32_t) * count) != cudaSuccess ||
+        cudaMallocHost(&m->h_flags, sizeof(uint32_t) * count) != cudaSuccess)
+        return bail(RAD_E_NOMEM);
+    cudaMemcpy(m->d_states, st.data(), sizeof(DevState*) * count, cudaMemcpyHostToDevice);
+    if (cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return bail(RAD_E_CUDA);
+    for (uint32_t i = 0; i < count; i++) {
+        cudaEventRecord(m->fork[i], m->stream);
+        cudaStreamWaitEvent(ctxs[i]->stream, m->fork[i], 0);
+        enqueue_batch(ctxs[i]);
+        cudaEventRecord(m->join[i], ctxs[i]->stream);
+        cudaStreamWaitEvent(m->stream, m->join[i], 0);
+    }
+    k_gather_flags<<<(count + 255) / 256, 256, 0, m->stream>>>(m->d_states, count, m->d_flags);
+    cudaMemcpyAsync(m->h_flags, m->d_flags, sizeof(uint32_t) * count, cudaMemcpyDeviceToHost, m->stream);
+    if (cudaStreamEndCapture(m->stream, &m->graph) != cudaSuccess) return bail(RAD_E_CUDA);
+    if (cudaGraphInstantiate(&m->exec, m->graph, 0) != cudaSuccess) return bail(RAD_E_CUDA);
+    *out = m;
+    return RAD_OK;
+}
+
+int rad_multi_shoot(rad_multi* m, uint32_t n_replays, uint32_t* stop_replay, double* stop_ms, uint32_t* replays,
+                    double* device_ms) {
+    if (!m) return RAD_E_INVALID;
+    const uint32_t count = (uint32_t)m->ctxs.size();
+    std::vector<uint32_t> at(count, 0);
+    std::vector<double> at_ms(count, 0.0);
+    double total = 0;
+    uint32_t done_replays = 0;
+    for (uint32_t r = 0; r < n_replays; r++) {
+        if (cudaEventRecord(m->t0, m->stream) != cudaSuccess) return RAD_E_CUDA;
+        if (cudaGraphLaunch(m->exec, m->stream) != cudaSuccess) return RAD_E_CUDA;
+        if (cudaEventRecord(m->t1, m->stream) != cudaSuccess) return RAD_E_CUDA;
+        if (cudaStreamSynchronize(m->stream) != cudaSuccess) return RAD_E_CUDA;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, m->t0, m->t1);
+        total += ms;
+        done_replays = r + 1;
+        uint32_t open = 0;
+        for (uint32_t i = 0; i < count; i++) {
+            if (m->h_flags[i] && !at[i]) {
+                at[i] = r + 1;
+                at_ms[i] = total;
+            }
+            open += at[i] == 0;
+        }
+        if (!open) break;
+    }
+    for (uint32_t i = 0; i < count; i++) {
+        DevState s;
+        cudaMemcpy(&s, m->ctxs[i]->d_state, sizeof(s), cudaMemcpyDeviceToHost);
+        if (s.overflow) return RAD_E_OVERFLOW;
+    }
+    if (stop_replay) std::memcpy(stop_replay, at.data(), sizeof(uint32_t) * count);
+    if (stop_ms) std::memcpy(stop_ms, at_ms.data(), sizeof(double) * count);
+    if (replays) *replays = done_replays;
+    if (device_ms) *device_ms = total;
+    return RAD_OK;
+}
+
 int rad_raster_counters(rad_ctx* c, uint64_t* out) {
     if (!c || !out) return RAD_E_INVALID;
     RAD_CUDA(c, cudaStreamSynchronize(c->stream));

@@ -164,9 +164,9 @@ def _concat(a: dict, b: dict) -> dict:
     return out
 
 
-def cornell_variant(target: int = 5000, seed: int = 0) -> dict:
+def cornell_variant(target: int = 5000, seed: int = 0, n_lights: int = 1) -> dict:
     """A seeded variation of ``cornell_box`` for training data: box size, block sizes and
-    positions, wall reflectances, and the light's size, position and emission vary."""
+    positions, wall reflectances, and the lights' sizes, positions and emission vary."""
     rng = np.random.default_rng(seed)
     S = float(rng.uniform(4.0, 7.0))
     zero = (0.0, 0.0, 0.0)
@@ -188,10 +188,13 @@ def cornell_variant(target: int = 5000, seed: int = 0) -> dict:
         r = rho()
         for f in _box_faces((x0, 0.0, z0), (x0 + w, min(h, 0.8 * S), z0 + d)):
             parts.append((f, r, zero, 5 + b))
-    lw, ld = rng.uniform(0.15, 0.35, 2) * S
-    lx = rng.uniform(0.1 * S, S - lw - 0.1 * S)
-    lz = rng.uniform(0.1 * S, S - ld - 0.1 * S)
-    em = tuple(rng.uniform(5.0, 20.0, 3))
-    light = _rect((lx, S - 0.005, lz), (lw, 0, 0), (0, 0, ld), np.array([0, -1.0, 0]))
+    lights = []
+    for k in range(n_lights):
+        lw, ld = rng.uniform(0.1, 0.3, 2) * S
+        lx = rng.uniform(0.05 * S, S - lw - 0.05 * S)
+        lz = rng.uniform(0.05 * S, S - ld - 0.05 * S)
+        em = tuple(rng.uniform(5.0, 20.0, 3))
+        light = _rect((lx, S - 0.005 - 0.001 * k, lz), (lw, 0, 0), (0, 0, ld), np.array([0, -1.0, 0]))
+        lights.append((light, (0.8, 0.8, 0.8), em, 7 + k))
     edge = _fit_edge(parts, target)
-    return _concat(_assemble(parts, edge), _assemble([(light, (0.8, 0.8, 0.8), em, 7)], edge))
+    return _concat(_assemble(parts, edge), _assemble(lights, edge))

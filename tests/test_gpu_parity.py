@@ -279,3 +279,25 @@ def test_lane_warp_split_is_exact(lib, orc, cornell, small):
     assert c["pairs"] > 0 and c["small_tris"] + c["big_tris"] <= c["pairs"]
     items = np.concatenate([orc.render(W, cornell["vertices"], int(p)) for p in sh])
     assert np.array_equal(_bits(F), _bits(orc.ff_exact(W, items, len(sh), n)))
+
+
+def test_multi_scene_graph_matches_single_runs(lib, orc):
+    """Scenes of uneven size advanced together in one graph give the same state, bit for
+    bit, as each scene solved alone, and each stops at the same shot as alone."""
+    from radiosity_gb300 import scenes
+
+    scs = [scenes.cornell_variant(t, seed=s) for t, s in ((600, 1), (1500, 2), (900, 3))]
+    solvers = []
+    for sc in scs:
+        s = solver(lib, sc, 32, 4, mode=1, tolerance=0.05)
+        solvers.append(s)
+    with lib.Multi(solvers) as mm:
+        at, ms, reps, total = mm.shoot(400)
+    assert np.all(at > 0) and reps == at.max() and total > 0
+    for sc, s, a in zip(scs, solvers, at):
+        rad, ill = s.download()
+        s.close()
+        orad, oill, ost = orc.shoot(1, 32, 4, sc["vertices"], sc["color"], sc["radiosity"], sc["illumination"], 400,
+                                    rho=sc["reflectance"], tol=0.05)
+        assert ost.stopped and ost.shots_done == a
+        assert np.array_equal(_bits(rad), _bits(orad)) and np.array_equal(_bits(ill), _bits(oill))
