@@ -54,6 +54,7 @@ def parse():
     p.add_argument("--workload", default="large", choices=["large", "small", "precision", "learned", "uneven"],
                    help="large: the headline plain configuration; the others are the other benchmark configs")
     p.add_argument("--fp64-solve", action="store_true", help="precision: also solve the full system in FP64 on CPU")
+    p.add_argument("--uneven-tol", type=float, default=1e-4, help="uneven: unshot-fraction tolerance per scene")
     p.add_argument("--headline-patches", type=int, default=50000,
                    help="learned: patch count of the time-to-1e-4 comparison scene (0 skips it)")
     return p.parse_args()
@@ -453,11 +454,14 @@ def run_learned(args):
 
 def headline(args, m):
     """Time to residual <= 1e-4 on one large scene: learned warm start + BF16 gather (dense capture
-    included) against the plain FP32 progressive shooter, both at W=args.w on this GPU.  The
-    shooter runs in segments of 16 batches; after each, its total radiosity (shot + unshot) is
-    checked with the residual ||E + rho o (F B) - B|| / ||E|| on the captured FP32 rows (untimed),
-    so both methods are stopped by the same criterion; the shooter's own unshot-power rule is
-    recorded beside it.  The final answers are checked in FP64 on the host."""
+    included) against the plain FP32 progressive shooter, both at W=args.w on this GPU.
+
+    Each method is stopped by the relative L2 residual of its own discrete system on the captured
+    FP32 rows: the gather solves B = E + rho o (F B); the shooter, which spreads power with the
+    reciprocity form F_ji = F_ij A_i / A_j, solves B = E + rho o (F^T (A o B)) / A.  The two fixed
+    points differ by the hemicube reciprocity error (reported).  The shooter runs in segments of
+    16 batches with its total radiosity (shot + unshot) checked after each (untimed); its own
+    unshot-power rule is recorded beside it.  Final answers are checked in FP64 on the host."""
     import radiosity_gb300 as R
     from radiosity_gb300 import learned, scenes
 
@@ -478,8 +482,8 @@ def headline(args, m):
     B, st = g.gather(E, guess=guess, tol=tol, max_outer=100, sweeps=4)
     _, st0 = g.gather(E, tol=tol, max_outer=100, sweeps=4)
 
-    def resid(Bt):  # Bt: N x 3
-        r = g.gather_residual(E, np.ascontiguousarray(Bt.T, np.float32))
+    def resid(Bt):  # Bt: N x 3, the shooter's own (reciprocity-form) system
+        r = g.shoot_residual(E, np.ascontiguousarray(Bt.T, np.float32))
         return float(np.linalg.norm(r.astype(np.float64)) / np.linalg.norm(E64))
 
     # plain shooter, same raster configuration
@@ -505,21 +509,29 @@ def headline(args, m):
             break
     s.close()
     # FP64 host residuals of both answers on the FP32 rows, in row blocks
+    v = sc["vertices"].reshape(n, 4, 3).astype(np.float64)
+    area = 0.5 * np.linalg.norm(np.cross(v[:, 0] - v[:, 2], v[:, 1] - v[:, 3]), axis=1)
     Bg = B.T.astype(np.float64)
     FBp = np.zeros((n, 3))
     FBg = np.zeros((n, 3))
+    FTp = np.zeros((n, 3))
     for r0 in range(0, n, 4096):
         F, _, _ = g.dense_rows(r0, min(4096, n - r0))
         Fd = F.astype(np.float64)
-        FBp[r0:r0 + len(F)] = Fd @ Bp
-        FBg[r0:r0 + len(F)] = Fd @ Bg
+        r1 = r0 + len(F)
+        FBp[r0:r1] = Fd @ Bp
+        FBg[r0:r1] = Fd @ Bg
+        FTp += Fd.T @ (area[r0:r1, None] * Bp[r0:r1])
     g.close()
-    res_p64 = float(np.linalg.norm(E64 + rho * FBp - Bp) / np.linalg.norm(E64))
-    res_g64 = float(np.linalg.norm(E64 + rho * FBg - Bg) / np.linalg.norm(E64))
+    nE = np.linalg.norm(E64)
+    res_p64 = float(np.linalg.norm(E64 + rho * FTp / area[:, None] - Bp) / nE)  # shooter, own system
+    res_p_gather = float(np.linalg.norm(E64 + rho * FBp - Bp) / nE)  # shooter answer, gather system
+    res_g64 = float(np.linalg.norm(E64 + rho * FBg - Bg) / nE)
+    rel_diff = float(np.linalg.norm(Bg - Bp) / np.linalg.norm(Bg))
     learned_s = (cap_ms + st.device_ms) / 1000 + (t2 - t1)
     return {"patches": n, "W": W, "K": int(args.k), "tol": tol,
             "plain": {"device_s": dev_ms / 1000, "batches": batches, "hemicubes": hemis,
-                      "residual": res_p, "fp64_residual": res_p64,
+                      "residual": res_p, "fp64_residual": res_p64, "gather_system_residual": res_p_gather,
                       "unshot_rule_s": None if t_unshot is None else t_unshot[0],
                       "unshot_rule_batches": None if t_unshot is None else t_unshot[1]},
             "learned_gather": {"capture_s": cap_ms / 1000, "predict_host_s": t2 - t1,
@@ -528,6 +540,7 @@ def headline(args, m):
                                "fp64_residual": res_g64, "total_s": learned_s},
             "gather_from_emission": {"solve_s": st0.device_ms / 1000, "outer": st0.outer, "sweeps": st0.sweeps,
                                      "initial_residual": st0.initial_residual},
+            "answers_rel_l2_difference": rel_diff,
             "speedup_learned_gather_vs_plain": (dev_ms / 1000) / learned_s}
 
 
@@ -538,34 +551,38 @@ def run_uneven(args):
     from radiosity_gb300 import scenes
 
     rng = np.random.default_rng(args.seed)
-    n_scenes, W, tol = 256, 128, 1e-2
+    n_scenes, W, tol = 256, 128, args.uneven_tol
     scs = []
     for k in range(n_scenes):
         target = int(np.exp(rng.uniform(np.log(500), np.log(8000))))
         scs.append(scenes.cornell_variant(target, seed=int(rng.integers(1 << 30)), n_lights=int(rng.integers(1, 4))))
     sizes = [sc["n"] for sc in scs]
+    # shooters per batch sized per scene so that all scenes need about the same number of replays
+    ks = R.plan_shooters(sizes, hemicubes_per_patch=2.0 if tol >= 1e-2 else 4.5)
 
-    def make(sc, **kw):
-        s = R.Solver(hemicube_side=W, hemicubes_count=8, mode=R.MODE_PHYS, tolerance=tol, **kw)
+    def make(sc, K, **kw):
+        s = R.Solver(hemicube_side=W, hemicubes_count=K, mode=R.MODE_PHYS, tolerance=tol, **kw)
         s.upload(sc["vertices"], sc["color"], sc["radiosity"], sc["illumination"], reflectance=sc["reflectance"])
         return s
 
     # the raster shape is tuned once, on the largest scene, and shared by every context
-    probe = make(scs[int(np.argmax(sizes))])
+    big = int(np.argmax(sizes))
+    probe = make(scs[big], ks[big])
     tune = probe.autotune()
     probe.close()
-    solvers = [make(sc, tile=tune.tile, small_tri_pixels=tune.small_tri_pixels) for sc in scs]
+    solvers = [make(sc, K, tile=tune.tile, small_tri_pixels=tune.small_tri_pixels) for sc, K in zip(scs, ks)]
     with R.Multi(solvers) as mm:
         at, ms, reps, total = mm.shoot(4000)
     done = at > 0
-    line = {"metric": "scenes/s (plain shooter to unshot fraction <= 1e-2, one CUDA graph)",
+    line = {"metric": f"scenes/s (plain shooter to unshot fraction <= {tol:g}, one CUDA graph)",
             "value": float(done.sum()) / (total / 1000), "unit": "scenes/s", "workload": "uneven",
             "higher_is_better": True, "scenes": n_scenes, "converged": int(done.sum()), "replays": reps,
             "device_s": total / 1000, "per_scene_ms": {"p50": float(np.percentile(ms[done], 50)),
                                                        "p99": float(np.percentile(ms[done], 99))},
             "patches": {"min": int(min(sizes)), "max": int(max(sizes)), "total": int(sum(sizes))},
-            "config": {"workload": f"{n_scenes} Cornell-variant scenes, W={W}, K=8, tol={tol}",
-                       "tile_from_autotune": tune.tile}, "data": "synthetic"}
+            "hemicubes": int(sum(int(a) * k for a, k in zip(at, ks))),
+            "config": {"workload": f"{n_scenes} Cornell-variant scenes, W={W}, K per scene {min(ks)}-{max(ks)} "
+                                   f"(plan_shooters), tol={tol:g}", "tile_from_autotune": tune.tile}, "data": "synthetic"}
     for s in solvers:
         s.close()
     print(json.dumps(line), flush=True)

@@ -180,6 +180,12 @@ int rad_gather_solve(rad_ctx* ctx, const float* emission, uint32_t R, const floa
  * this is the first-shot direct light rho o (F E). */
 int rad_gather_residual(rad_ctx* ctx, const float* emission, uint32_t R, const float* radiosity, float* residual);
 
+/* Residual of the system the progressive shooter solves, r_j = E_j + rho_j (sum_i F_ij A_i B_i)
+ * / A_j - B_j (reciprocity form of the shoot update, source/Main.cpp:1268-1276), on the FP32
+ * rows, same arrays as rad_gather_residual.  The two discretisations differ by the hemicube
+ * reciprocity error, so each method is checked against its own system. */
+int rad_shoot_residual(rad_ctx* ctx, const float* emission, uint32_t R, const float* radiosity, float* residual);
+
 /* Diagnostic: C = A * Bt^T on the tcgen05 path (A n x k, Bt R x k BF16 bits, row-major;
  * C column-major R x n FP32), on `device`. */
 int rad_bf16_gemm(int device, const uint16_t* A, const uint16_t* Bt, uint32_t n, uint32_t k, uint32_t R, float* C);

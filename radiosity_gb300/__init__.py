@@ -7,7 +7,7 @@ with ctypes.  Scene generators for the synthetic benchmark workloads live in
 """
 from ._lib import (  # noqa: F401
     EXPORTS, MLP, MODE_PHYS, MODE_REF, Multi, RadConfig, RadError, RadGatherStats, RadStats, RadTuning, Solver, bf16_gemm,
-    default_config, derived, load,
+    default_config, derived, load, plan_shooters,
     reference_scene,
 )
 from .build import LIB as LIB_PATH  # noqa: F401

@@ -33,7 +33,7 @@ EXPORTS = [
     "rad_set_state", "rad_download", "rad_ff_table", "rad_select_shooters", "rad_render_item_buffers",
     "rad_reduce_item_buffers", "rad_ff_rows", "rad_shoot", "rad_profile_stages", "rad_scene_reference",
     "rad_reduce_items_noalloc", "rad_raster_counters", "rad_autotune", "rad_dense_capture",
-    "rad_dense_rows", "rad_gather_solve", "rad_gather_residual", "rad_bf16_gemm", "rad_mlp_create", "rad_mlp_destroy",
+    "rad_dense_rows", "rad_gather_solve", "rad_gather_residual", "rad_shoot_residual", "rad_bf16_gemm", "rad_mlp_create", "rad_mlp_destroy",
     "rad_mlp_param_count", "rad_mlp_get_params", "rad_mlp_set_params", "rad_mlp_predict", "rad_mlp_gradients",
     "rad_mlp_train", "rad_multi_create", "rad_multi_shoot", "rad_multi_destroy", "rad_strerror", "rad_last_error",
 ]
@@ -131,6 +131,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rad_gather_solve.argtypes = [vp, _f32p, ctypes.c_uint32, vp, ctypes.c_double, ctypes.c_uint32,
                                    ctypes.c_uint32, _f32p, P(RadGatherStats)]
     L.rad_gather_residual.argtypes = [vp, _f32p, ctypes.c_uint32, _f32p, _f32p]
+    L.rad_shoot_residual.argtypes = [vp, _f32p, ctypes.c_uint32, _f32p, _f32p]
     L.rad_bf16_gemm.argtypes = [ctypes.c_int, vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _f32p]
     L.rad_mlp_create.argtypes = [ctypes.c_int, ctypes.c_uint64, P(vp)]
     L.rad_mlp_destroy.argtypes = [vp]
@@ -360,6 +361,15 @@ class Solver:
                     "rad_gather_residual")
         return r
 
+    def shoot_residual(self, emission, radiosity):
+        """rad_shoot_residual: r = E + rho o (F^T (A o B)) / A - B, the shooter's own system."""
+        E = np.ascontiguousarray(emission, np.float32)
+        B = np.ascontiguousarray(radiosity, np.float32)
+        r = np.zeros_like(E)
+        self._check(self.L.rad_shoot_residual(self.h, E.reshape(-1), E.shape[0], B.reshape(-1), r.reshape(-1)),
+                    "rad_shoot_residual")
+        return r
+
     RASTER_COUNTERS = ["pairs", "small_tris", "small_px", "big_tris", "big_stamps", "stamps_visited",
                        "stamps_inside", "big_px_written"]
 
@@ -439,6 +449,25 @@ class MLP:
         if rc:
             raise RadError(rc, "rad_mlp_train")
         return loss.value, ms.value
+
+
+def plan_shooters(patches, hemicubes_per_patch: float = 2.0, replays: int = 128, kmin: int = 8,
+                  kmax: int = 128) -> list:
+    """Shooters per batch for each scene of an uneven batch solved under one graph.
+
+    Every replay of the graph advances every scene by one batch, so the batch ends when the
+    scene that needs the most replays converges.  A scene of N patches needs about
+    ``hemicubes_per_patch * N`` hemicubes to reach its tolerance (about 2 for an unshot fraction
+    of 1e-2 and 4.5 for 1e-4 on the Cornell-style scenes), hence K = that / ``replays``, rounded
+    up to a power of two and clamped to [kmin, kmax], makes the scenes finish together."""
+    out = []
+    for n in patches:
+        want = max(1.0, hemicubes_per_patch * float(n) / replays)
+        k = 1
+        while k < want:
+            k *= 2
+        out.append(int(min(max(k, kmin), kmax)))
+    return out
 
 
 class Multi:

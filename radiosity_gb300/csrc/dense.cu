@@ -125,6 +125,67 @@ void launch_sgemm_resid(const float* F, uint32_t n, uint32_t ld, const float* X,
     k_sgemm_resid<<<grid, 256, 0, s>>>(F, n, ld, X, E, rho, R, r, nrm);
 }
 
+// ---------------------------------------------------------------------------
+// Shooting-form residual: the progressive shooter distributes patch i's power with
+// F_ji = F_ij A_i / A_j (source/Main.cpp:1268-1276 with the area ratio), so its fixed
+// point solves B_j = E_j + rho_j (sum_i F_ij A_i B_i) / A_j.  k_colsum_area forms
+// acc[c][j] += sum_i F_ij A_i X[c][i] over a slab of 1024 rows per CTA row (FP32 in
+// the slab, FP64 atomics across slabs); k_shoot_resid finishes r.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kColSlab = 1024;
+constexpr uint32_t kColRhs = 4;
+
+__global__ void __launch_bounds__(256) k_colsum_area(const float* __restrict__ F, uint32_t n, uint32_t ld,
+                                                     const float* __restrict__ X, const float* __restrict__ area,
+                                                     uint32_t R, uint32_t c0, double* acc) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i0 = blockIdx.y * kColSlab, i1 = min(n, i0 + kColSlab);
+    const uint32_t nc = min(kColRhs, R - c0);
+    __shared__ float y[kColRhs][64];
+    float s[kColRhs] = {0.f, 0.f, 0.f, 0.f};
+    for (uint32_t b0 = i0; b0 < i1; b0 += 64) {
+        __syncthreads();
+        for (uint32_t e = threadIdx.x; e < kColRhs * 64; e += blockDim.x) {
+            const uint32_t c = e / 64, i = b0 + e % 64;
+            y[c][e % 64] = (c < nc && i < i1) ? area[i] * X[(size_t)(c0 + c) * n + i] : 0.f;
+        }
+        __syncthreads();
+        if (j < n) {
+            const uint32_t m = min(64u, i1 - b0);
+            for (uint32_t q = 0; q < m; q++) {
+                const float f = F[(size_t)(b0 + q) * ld + j];
+#pragma unroll
+                for (uint32_t c = 0; c < kColRhs; c++) s[c] = fmaf(f, y[c][q], s[c]);
+            }
+        }
+    }
+    if (j < n)
+        for (uint32_t c = 0; c < nc; c++) atomicAdd(&acc[(size_t)(c0 + c) * n + j], (double)s[c]);
+}
+
+__global__ void k_shoot_resid(const double* __restrict__ acc, const float* __restrict__ X, const float* __restrict__ E,
+                              const float4* __restrict__ rho, const float* __restrict__ area, uint32_t n, uint32_t R,
+                              float* r) {
+    const size_t total = (size_t)n * R;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t c = (uint32_t)(e / n), j = (uint32_t)(e % n);
+        const float4 rh = rho[j];
+        const int ch = (int)(c % 3);
+        const double rr = ch == 0 ? rh.x : (ch == 1 ? rh.y : rh.z);
+        const double a = area[j];
+        const double v = (double)E[e] + (a > 0 ? rr * acc[e] / a : 0.0) - (double)X[e];
+        r[e] = (float)v;
+    }
+}
+
+void launch_shoot_resid(const float* F, uint32_t n, uint32_t ld, const float* X, const float* E, const float4* rho,
+                        const float* area, uint32_t R, double* acc, float* r, cudaStream_t s) {
+    cudaMemsetAsync(acc, 0, sizeof(double) * (size_t)n * R, s);
+    dim3 grid((n + 255) / 256, (n + kColSlab - 1) / kColSlab);
+    for (uint32_t c0 = 0; c0 < R; c0 += kColRhs) k_colsum_area<<<grid, 256, 0, s>>>(F, n, ld, X, area, R, c0, acc);
+    k_shoot_resid<<<152 * 4, 256, 0, s>>>(acc, X, E, rho, area, n, R, r);
+}
+
 // BF16 transposed copy of a column-major N x R block: Xt[c][j] (ld columns, zero padded).
 __global__ void k_pack_bf16(const float* __restrict__ X, uint32_t n, uint32_t R, uint32_t ld, __nv_bfloat16* Xt,
                             uint32_t Rpad) {

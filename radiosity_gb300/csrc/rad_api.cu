@@ -709,7 +709,7 @@ int rad_autotune(rad_ctx* c, uint32_t flags, rad_tuning* out) {
     const uint32_t want = std::max<uint32_t>(8, std::min<uint32_t>(K0, 64));
     for (uint32_t i = 0; sh.size() < want && i < want; i++) sh.push_back((uint32_t)(((uint64_t)i * 2654435761u) % c->n));
     const uint32_t tiles[3] = {16, 32, 64};
-    const uint32_t smalls[5] = {16, 32, 64, 128, 256};
+    const uint32_t smalls[7] = {16, 32, 64, 128, 256, 512, 1024};
     uint32_t best_t = 0, best_s = 0, cand = 0;
     float best = 1e30f;
     for (uint32_t t : tiles) {
@@ -953,6 +953,31 @@ int rad_gather_residual(rad_ctx* c, const float* emission, uint32_t R, const flo
     cudaFree(dE);
     cudaFree(dB);
     cudaFree(dr);
+    return rc;
+}
+
+int rad_shoot_residual(rad_ctx* c, const float* emission, uint32_t R, const float* radiosity, float* residual) {
+    if (!c || !emission || !radiosity || !residual || R == 0) return RAD_E_INVALID;
+    if (!c->dense_ready || !c->d_F32) return fail(c, RAD_E_STATE, "needs rad_dense_capture with RAD_DENSE_FP32");
+    const size_t nr = (size_t)c->n * R;
+    float *dE = nullptr, *dB = nullptr, *dr = nullptr;
+    double* dacc = nullptr;
+    int rc = RAD_OK;
+    if (cudaMalloc(&dE, 4 * nr) != cudaSuccess || cudaMalloc(&dB, 4 * nr) != cudaSuccess ||
+        cudaMalloc(&dr, 4 * nr) != cudaSuccess || cudaMalloc(&dacc, 8 * nr) != cudaSuccess)
+        rc = fail(c, RAD_E_NOMEM, "residual buffers");
+    if (!rc) {
+        cudaMemcpyAsync(dE, emission, 4 * nr, cudaMemcpyHostToDevice, c->stream);
+        cudaMemcpyAsync(dB, radiosity, 4 * nr, cudaMemcpyHostToDevice, c->stream);
+        launch_shoot_resid(c->d_F32, c->n, c->dense_ld, dB, dE, c->d_rho, c->d_area, R, dacc, dr, c->stream);
+        cudaMemcpyAsync(residual, dr, 4 * nr, cudaMemcpyDeviceToHost, c->stream);
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(c->stream) != cudaSuccess)
+            rc = fail(c, RAD_E_CUDA, "shooting-form residual failed");
+    }
+    cudaFree(dE);
+    cudaFree(dB);
+    cudaFree(dr);
+    cudaFree(dacc);
     return rc;
 }
 

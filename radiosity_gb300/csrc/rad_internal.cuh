@@ -138,6 +138,8 @@ void launch_dense_rows(const unsigned long long* Fq, uint32_t count, uint32_t n,
                        float* F32, __nv_bfloat16* F16, float* scale, cudaStream_t s);
 void launch_sgemm_resid(const float* F, uint32_t n, uint32_t ld, const float* X, const float* E, const float4* rho,
                         uint32_t R, float* r, double* nrm, cudaStream_t s);
+void launch_shoot_resid(const float* F, uint32_t n, uint32_t ld, const float* X, const float* E, const float4* rho,
+                        const float* area, uint32_t R, double* acc, float* r, cudaStream_t s);
 void launch_pack_bf16(const float* X, uint32_t n, uint32_t R, uint32_t ld, __nv_bfloat16* Xt, uint32_t Rpad,
                       cudaStream_t s);
 void launch_axpy(float* y, const float* x, size_t total, cudaStream_t s);

@@ -238,6 +238,29 @@ __device__ __forceinline__ void count_bins(const Geo& g, const Batch& b, uint32_
         for (int c = c0; c <= c1; c++) atomicAdd(&cnt[r * F.bins_x + c], 1u);
 }
 
+// count_bins for the fast path, called by all 32 lanes: triangles that touch a
+// single bin (most of them) are grouped by bin with __match_any_sync and counted
+// with one atomic per group; the others count their bins one by one.
+__device__ __forceinline__ void count_bins_warp(const Geo& g, const Batch& b, uint32_t hi, const FaceInfo& F,
+                                                const int* px, bool on) {
+    const int tile = (int)g.tile;
+    int c0 = 0, c1 = -1, r0 = 0, r1 = -1;
+    if (on) {
+        c0 = (px[0] - F.sc[0]) / tile;
+        c1 = (px[1] - F.sc[0]) / tile;
+        r0 = (px[2] - F.sc[1]) / tile;
+        r1 = (px[3] - F.sc[1]) / tile;
+    }
+    uint32_t* cnt = b.bin_count + (size_t)hi * g.nb + F.bin_base;
+    const bool single = on && c0 == c1 && r0 == r1;
+    const uint32_t key = single ? (uint32_t)(r0 * F.bins_x + c0) : 0xFFFFFFFFu;
+    const unsigned grp = __match_any_sync(0xffffffffu, key);
+    if (single && (threadIdx.x & 31) == (unsigned)(__ffs(grp) - 1)) atomicAdd(&cnt[key], (uint32_t)__popc(grp));
+    if (on && !single)
+        for (int r = r0; r <= r1; r++)
+            for (int c = c0; c <= c1; c++) atomicAdd(&cnt[r * F.bins_x + c], 1u);
+}
+
 // Snap one clip-space vertex to 24.8 fixed-point window coordinates; false when w <= 0.
 __device__ __forceinline__ bool snap_vertex(float4 c, float hw, float hh, float vx, float vy, SV& o) {
     if (!(c.w > 0)) return false;
@@ -273,7 +296,7 @@ __device__ __noinline__ void emit_polygon(const Geo& g, const Batch& b, const fl
     }
 }
 
-__global__ void __launch_bounds__(128, 5) k_setup(Geo g, Batch b, const float* __restrict__ verts, DevState* st) {
+__global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* __restrict__ verts, DevState* st) {
     if (st->stopped) return;
     const uint32_t hi = blockIdx.y;
     if (!b.valid[hi]) return;
@@ -358,16 +381,14 @@ __global__ void __launch_bounds__(128, 5) k_setup(Geo g, Batch b, const float* _
             }
             const uint32_t ncand = fast ? (ok ? 1u : 0u) : (pn >= 3 ? (uint32_t)(pn - 2) : 0u);
             const uint32_t base = warp_alloc(&st->tri_count, ncand);
+            const bool written = fast && ok && base < b.tri_cap;
             if (fast && ok) {
-                if (base >= b.tri_cap) {
-                    atomicOr(&st->overflow, 1u);
-                } else {
-                    tri_write(s0, s1, s2, p, hi * 5 + (uint32_t)f, F, px, &b.tris[base]);
-                    count_bins(g, b, hi, F, px);
-                }
+                if (base >= b.tri_cap) atomicOr(&st->overflow, 1u);
+                else tri_write(s0, s1, s2, p, hi * 5 + (uint32_t)f, F, px, &b.tris[base]);
             } else if (ncand) {
                 emit_polygon(g, b, poly, pn, base, p, hi, f, hw, hh, vx, vy, st);
             }
+            count_bins_warp(g, b, hi, F, px, written);
         }
     }
 }
@@ -410,21 +431,49 @@ __global__ void k_fill(Geo g, Batch b, DevState* st) {
     if (st->stopped) return;
     const uint32_t ntri = min(st->tri_count, b.tri_cap);
     const int tile = (int)g.tile;
-    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < ntri; s += gridDim.x * blockDim.x) {
-        const TriRec& t = b.tris[s];
-        if (t.id == kDeadTri) continue;
-        uint32_t hi = t.hf / 5, f = t.hf % 5;
-        const FaceInfo& F = g.face[f];
-        int c0 = (t.px0 - F.sc[0]) / tile, c1 = (t.px1 - F.sc[0]) / tile;
-        int r0 = (t.py0 - F.sc[1]) / tile, r1 = (t.py1 - F.sc[1]) / tile;
-        size_t gb0 = (size_t)hi * g.nb + F.bin_base;
-        for (int r = r0; r <= r1; r++)
-            for (int c = c0; c <= c1; c++) {
-                size_t gb = gb0 + r * F.bins_x + c;
-                uint32_t pos = atomicAdd(&b.bin_fill[gb], 1u);
-                uint32_t idx = b.bin_offset[gb] + pos;
-                if (idx < b.list_cap) b.bin_list[idx] = s;
+    const uint32_t lane = threadIdx.x & 31;
+    // warp-uniform trip count so that single-bin triangles can be grouped by bin
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t s0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); s0 < ntri; s0 += stride) {
+        const uint32_t s = s0 + lane;
+        bool on = s < ntri;
+        int c0 = 0, c1 = -1, r0 = 0, r1 = -1;
+        size_t gb0 = 0;
+        uint32_t bins_x = 0;
+        if (on) {
+            const TriRec& t = b.tris[s];
+            on = t.id != kDeadTri;
+            if (on) {
+                const uint32_t hi = t.hf / 5, f = t.hf % 5;
+                const FaceInfo& F = g.face[f];
+                c0 = (t.px0 - F.sc[0]) / tile;
+                c1 = (t.px1 - F.sc[0]) / tile;
+                r0 = (t.py0 - F.sc[1]) / tile;
+                r1 = (t.py1 - F.sc[1]) / tile;
+                gb0 = (size_t)hi * g.nb + F.bin_base;
+                bins_x = F.bins_x;
             }
+        }
+        const bool single = on && c0 == c1 && r0 == r1;
+        const size_t gb1 = gb0 + (size_t)r0 * bins_x + c0;
+        const unsigned long long key = single ? (unsigned long long)gb1 : ~0ull;
+        const unsigned grp = __match_any_sync(0xffffffffu, key);
+        if (single) {
+            const int leader = __ffs(grp) - 1;
+            uint32_t pos = 0;
+            if ((int)lane == leader) pos = atomicAdd(&b.bin_fill[gb1], (uint32_t)__popc(grp));
+            pos = __shfl_sync(grp, pos, leader) + __popc(grp & ((1u << lane) - 1u));
+            const uint32_t idx = b.bin_offset[gb1] + pos;
+            if (idx < b.list_cap) b.bin_list[idx] = s;
+        } else if (on) {
+            for (int r = r0; r <= r1; r++)
+                for (int c = c0; c <= c1; c++) {
+                    const size_t gb = gb0 + (size_t)r * bins_x + c;
+                    const uint32_t pos = atomicAdd(&b.bin_fill[gb], 1u);
+                    const uint32_t idx = b.bin_offset[gb] + pos;
+                    if (idx < b.list_cap) b.bin_list[idx] = s;
+                }
+        }
     }
 }
 
@@ -457,7 +506,8 @@ constexpr int32_t kSmallExtent = 16384;  // 64 px in 24.8 fixed point: edge valu
 constexpr int kChunk = 256;          // triangle records staged per CTA round
 constexpr int kHashSlots = 1024;     // per-bin id -> sum table of the reduction phase
 constexpr uint32_t kHashEmpty = 0xFFFFFFFFu;
-constexpr int kRegionBytes = 12 * kHashSlots;  // >= kChunk * sizeof(RTri) (10 KB)
+constexpr int kRegionBytes = 12 * kHashSlots;  // >= kChunk * (sizeof(RTri) + 8) (12 KB)
+constexpr int kSizeClasses = 16;               // ceil(log2(box pixels)) for boxes <= 2^15 px
 
 // The parts of a triangle record the per-pixel loops need (40 bytes in shared memory).
 struct RTri {
@@ -465,43 +515,54 @@ struct RTri {
     float c0, ax, ay;
     uint32_t id;
 };
+static_assert(kChunk * (sizeof(RTri) + sizeof(short4)) <= (size_t)kRegionBytes, "chunk staging exceeds the region");
+static_assert(kChunk <= 256, "chunk indices are stored as uint8");
 
 __device__ __forceinline__ bool inside_edge(long long e, bool tl) { return e > 0 || (e == 0 && tl); }
 __device__ __forceinline__ bool inside_edge32(int32_t e, bool tl) { return e > 0 || (e == 0 && tl); }
 
 // One lane rasterises a small triangle over its clamped bbox [x0,x1]x[y0,y1] with
-// 32-bit incremental edge functions (exact: |E| < 2^30 for extents <= 64 px).
+// 32-bit incremental edge functions (exact: |E| < 2^30 for extents <= 64 px).  The
+// bbox is walked as one flat loop of w*h steps, so a warp runs max(w*h) steps over
+// its lanes (a nested row/column loop would run about max(h) * max(w)).
 template <int TILE>
 __device__ __forceinline__ void raster_small(const RTri& t, int x0, int x1, int y0, int y1, const BinInfo& bi, int sx,
                                              int sy, unsigned long long* key) {
-    int32_t er[3], stx[3], sty[3];
+    int32_t er[3], e[3], stx[3], sty[3];
     bool tl[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         const int j = k == 2 ? 0 : k + 1;
         const int32_t dx = t.X[j] - t.X[k], dy = t.Y[j] - t.Y[k];
         er[k] = dx * (y0 * 256 + 128 - t.Y[k]) - dy * (x0 * 256 + 128 - t.X[k]);
+        e[k] = er[k];
         stx[k] = -dy * 256;
         sty[k] = dx * 256;
         tl[k] = (t.Y[j] < t.Y[k]) || (t.Y[j] == t.Y[k] && t.X[j] < t.X[k]);
     }
-    for (int py = y0; py <= y1; py++) {
-        int32_t e0 = er[0], e1 = er[1], e2 = er[2];
-        const float w = (float)(py - sy);
-        for (int px = x0; px <= x1; px++) {
-            if (inside_edge32(e0, tl[0]) && inside_edge32(e1, tl[1]) && inside_edge32(e2, tl[2])) {
-                const float u = (float)(px - sx);
-                const float D = (t.c0 + t.ax * u) + t.ay * w;
-                const unsigned long long k = ((unsigned long long)depth_ordinal(D) << 32) | t.id;
-                atomicMin(&key[(py - bi.y0) * TILE + (px - bi.x0)], k);
-            }
-            e0 += stx[0];
-            e1 += stx[1];
-            e2 += stx[2];
+    const int steps = (x1 - x0 + 1) * (y1 - y0 + 1);
+    int px = x0, py = y0;
+    int row = (py - bi.y0) * TILE - (int)bi.x0;  // key index of pixel (px, py) = row + px
+    for (int i = 0; i < steps; i++) {
+        if (inside_edge32(e[0], tl[0]) && inside_edge32(e[1], tl[1]) && inside_edge32(e[2], tl[2])) {
+            const float u = (float)(px - sx), w = (float)(py - sy);
+            const float D = (t.c0 + t.ax * u) + t.ay * w;
+            atomicMin(&key[row + px], ((unsigned long long)depth_ordinal(D) << 32) | t.id);
         }
-        er[0] += sty[0];
-        er[1] += sty[1];
-        er[2] += sty[2];
+        if (px < x1) {
+            px++;
+#pragma unroll
+            for (int k = 0; k < 3; k++) e[k] += stx[k];
+        } else {
+            px = x0;
+            py++;
+            row += TILE;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                er[k] += sty[k];
+                e[k] = er[k];
+            }
+        }
     }
 }
 
@@ -581,7 +642,7 @@ __device__ __forceinline__ void raster_big(const RTri& t, int x0, int x1, int y0
 }
 
 template <int TILE>
-__global__ void __launch_bounds__(256, 3) k_raster(Geo g, Batch b, const float* __restrict__ fftab, DevState* st,
+__global__ void __launch_bounds__(256, 4) k_raster(Geo g, Batch b, const float* __restrict__ fftab, DevState* st,
                                                    int write_items, int fused, int count) {
     if (st->stopped) return;
     const uint32_t gb = blockIdx.x;
@@ -589,11 +650,15 @@ __global__ void __launch_bounds__(256, 3) k_raster(Geo g, Batch b, const float* 
     const BinInfo bi = b.bins[bin];
     const bool valid = b.valid[hi] != 0;
     __shared__ unsigned long long key[TILE * TILE];
-    // one region, two uses: big-triangle staging during the raster phase, then the
-    // per-bin id -> exact-sum hash table of the reduction phase
+    // one region, two uses: the chunk's triangles (records + clamped boxes) during the
+    // raster phase, then the per-bin id -> exact-sum hash table of the reduction phase
     __shared__ __align__(16) unsigned char s_region[kRegionBytes];
-    RTri* s_big = reinterpret_cast<RTri*>(s_region);
-    __shared__ int s_nbig;
+    RTri* s_tri = reinterpret_cast<RTri*>(s_region);
+    short4* s_box = reinterpret_cast<short4*>(s_region + kChunk * sizeof(RTri));
+    __shared__ uint8_t s_order[kChunk];  // small triangles by size class (ascending)
+    __shared__ uint8_t s_bigi[kChunk];   // big triangles
+    __shared__ uint32_t s_ncls[kSizeClasses];
+    __shared__ int s_nbig, s_nsmall;
     __shared__ uint32_t s_cnt[8];
     uint32_t* ctr = count ? s_cnt : nullptr;
     if (threadIdx.x < 8) s_cnt[threadIdx.x] = 0;
@@ -609,8 +674,13 @@ __global__ void __launch_bounds__(256, 3) k_raster(Geo g, Batch b, const float* 
         const int bx1 = bi.x0 + bi.w - 1, by1 = bi.y0 + bi.h - 1;
         for (uint32_t base = 0; base < cnt; base += kChunk) {
             const uint32_t m = min((uint32_t)kChunk, cnt - base);
+            if (threadIdx.x < kSizeClasses) s_ncls[threadIdx.x] = 0;
             if (threadIdx.x == 0) s_nbig = 0;
             __syncthreads();
+            // 1. load, clamp to the bin, split small (one lane) / big (one warp); small
+            //    triangles are counted per size class ceil(log2(box pixels))
+            int cls = -1;
+            uint32_t rank = 0;
             if (threadIdx.x < m) {
                 const TriRec& tr = b.tris[b.bin_list[off + base + threadIdx.x]];
                 const int4 a = *reinterpret_cast<const int4*>(&tr.X0);
@@ -625,25 +695,48 @@ __global__ void __launch_bounds__(256, 3) k_raster(Geo g, Batch b, const float* 
                 const int x0 = max(px0, (int)bi.x0), x1 = min(px1, bx1);
                 const int y0 = max(py0, (int)bi.y0), y1 = min(py1, by1);
                 if (x0 <= x1 && y0 <= y1) {
+                    s_tri[threadIdx.x] = t;
                     const int32_t ex = max(t.X[0], max(t.X[1], t.X[2])) - min(t.X[0], min(t.X[1], t.X[2]));
                     const int32_t ey = max(t.Y[0], max(t.Y[1], t.Y[2])) - min(t.Y[0], min(t.Y[1], t.Y[2]));
                     const int area = (x1 - x0 + 1) * (y1 - y0 + 1);
                     if (ex <= kSmallExtent && ey <= kSmallExtent && area <= (int)g.small_max) {
-                        raster_small<TILE>(t, x0, x1, y0, y1, bi, sx, sy, key);
+                        s_box[threadIdx.x] = make_short4((short)x0, (short)x1, (short)y0, (short)y1);
+                        cls = area > 1 ? 32 - __clz(area - 1) : 0;
+                        rank = atomicAdd(&s_ncls[cls], 1u);
                         if (ctr) {
                             atomicAdd(&ctr[1], 1u);
                             atomicAdd(&ctr[2], (uint32_t)area);
                         }
                     } else {
-                        s_big[atomicAdd(&s_nbig, 1)] = t;
+                        s_bigi[atomicAdd(&s_nbig, 1)] = (uint8_t)threadIdx.x;
                         if (ctr) atomicAdd(&ctr[3], 1u);
                     }
                 }
             }
             __syncthreads();
-            const int nbig = s_nbig;
+            // 2. class bases (exclusive scan of kSizeClasses counters)
+            if (threadIdx.x == 0) {
+                uint32_t run = 0;
+                for (int k = 0; k < kSizeClasses; k++) {
+                    const uint32_t v = s_ncls[k];
+                    s_ncls[k] = run;
+                    run += v;
+                }
+                s_nsmall = (int)run;
+            }
+            __syncthreads();
+            if (cls >= 0) s_order[s_ncls[cls] + rank] = (uint8_t)threadIdx.x;
+            __syncthreads();
+            // 3. small triangles, one per lane, in size order: a warp's lanes walk boxes of
+            //    similar size; then big triangles, one per warp (no barrier between)
+            const int nsmall = s_nsmall, nbig = s_nbig;
+            if ((int)threadIdx.x < nsmall) {
+                const int i = s_order[threadIdx.x];
+                const short4 bx = s_box[i];
+                raster_small<TILE>(s_tri[i], bx.x, bx.y, bx.z, bx.w, bi, sx, sy, key);
+            }
             for (int i = warp; i < nbig; i += nwarp) {
-                const RTri t = s_big[i];
+                const RTri t = s_tri[s_bigi[i]];
                 const int32_t xmn = min(t.X[0], min(t.X[1], t.X[2])), xmx = max(t.X[0], max(t.X[1], t.X[2]));
                 const int32_t ymn = min(t.Y[0], min(t.Y[1], t.Y[2])), ymx = max(t.Y[0], max(t.Y[1], t.Y[2]));
                 const int x0 = max((int)floordiv256((long long)xmn - 128 + 255), (int)bi.x0);

@@ -79,3 +79,38 @@ def test_gather_solve_matches_fp64(lib, box):
         A = np.eye(n) - rho[:, c % 3][:, None] * F64
         ref = np.linalg.solve(A, E[c].astype(np.float64))
         assert np.linalg.norm(B[c] - ref) <= 1e-5 * np.linalg.norm(ref)
+
+
+def test_shoot_residual_matches_fp64_and_the_shooter_converges_on_it(lib, box):
+    """rad_shoot_residual equals the FP64 reciprocity-form residual, and the plain shooter's
+    total radiosity (shot + unshot) drives it down as the unshot fraction falls."""
+    from radiosity_gb300 import learned
+
+    n = box["n"]
+    rng = np.random.default_rng(9)
+    E = learned.emission_block(box)
+    X = (E + rng.uniform(0, 0.5, E.shape)).astype(np.float32)
+    rho = box["reflectance"].reshape(n, 3).astype(np.float64)
+    with _solver(lib, box) as s:
+        s.dense_capture(keep_fp32=True)
+        F, _, _ = s.dense_rows(0, n)
+        r = s.shoot_residual(E, X)
+        v = box["vertices"].reshape(n, 4, 3).astype(np.float64)
+        area = 0.5 * np.linalg.norm(np.cross(v[:, 0] - v[:, 2], v[:, 1] - v[:, 3]), axis=1)
+        y = (X.astype(np.float64) * area[None, :])
+        FT = F.astype(np.float64).T @ y.T  # N x 3
+        ref = E.astype(np.float64) + (rho * FT / area[:, None]).T - X
+        assert np.max(np.abs(r - ref)) <= 1e-5 * np.max(np.abs(ref))
+        # the shooter's own system
+        res = []
+        for tol in (1e-2, 1e-4):
+            sh = lib.Solver(hemicube_side=64, hemicubes_count=16, mode=1, tolerance=tol)
+            sh.upload(box["vertices"], box["color"], box["radiosity"], box["illumination"],
+                      reflectance=box["reflectance"])
+            st = sh.shoot(5000)
+            rad, ill = sh.download()
+            sh.close()
+            assert st.stopped
+            Bt = (rad.astype(np.float64) + ill).reshape(n, 3).T.astype(np.float32)
+            res.append(np.linalg.norm(s.shoot_residual(E, Bt).astype(np.float64)) / np.linalg.norm(E))
+        assert res[1] < 0.1 * res[0] and res[1] < 1e-3
