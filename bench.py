@@ -47,6 +47,7 @@ def parse():
     p.add_argument("--w", type=int, default=512, help="hemicube side")
     p.add_argument("--patches", type=int, default=50000)
     p.add_argument("--tile", type=int, default=0)
+    p.add_argument("--small", type=int, default=0, help="lane/warp triangle split in box pixels (0: default)")
     p.add_argument("--seed", type=int, default=0)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -228,7 +229,8 @@ def run_ours(args):
     sc = workload(args)
     K, W = args.k, args.w
     n = sc["n"]
-    solver = R.Solver(hemicube_side=W, hemicubes_count=K, mode=R.MODE_PHYS, tile=args.tile, device=dev)
+    solver = R.Solver(hemicube_side=W, hemicubes_count=K, mode=R.MODE_PHYS, tile=args.tile,
+                      small_tri_pixels=args.small, device=dev)
     solver.upload(sc["vertices"], sc["color"], sc["radiosity"], sc["illumination"], reflectance=sc["reflectance"])
 
     def barrier():
