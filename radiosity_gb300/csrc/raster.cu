@@ -521,6 +521,26 @@ static_assert(kChunk <= 256, "chunk indices are stored as uint8");
 __device__ __forceinline__ bool inside_edge(long long e, bool tl) { return e > 0 || (e == 0 && tl); }
 __device__ __forceinline__ bool inside_edge32(int32_t e, bool tl) { return e > 0 || (e == 0 && tl); }
 
+// Adds an exact partial sum to the bin's open-addressing id -> sum table (linear probing,
+// at most 32 probes); a crowded table sends the sum straight to the global row.
+__device__ __forceinline__ void hash_add(uint32_t* h_id, unsigned long long* h_sum, unsigned long long* Fq,
+                                         uint32_t id, unsigned long long sum) {
+    uint32_t slot = (id * 2654435761u) >> 22;
+    for (int probe = 0; probe < 32; probe++) {
+        uint32_t cur = h_id[slot];
+        if (cur == kHashEmpty) {
+            cur = atomicCAS(&h_id[slot], kHashEmpty, id);
+            if (cur == kHashEmpty) cur = id;
+        }
+        if (cur == id) {
+            atomicAdd(&h_sum[slot], sum);
+            return;
+        }
+        slot = (slot + 1) & (kHashSlots - 1);
+    }
+    atomicAdd(&Fq[id], sum);
+}
+
 // One lane rasterises a small triangle over its clamped bbox [x0,x1]x[y0,y1] with
 // 32-bit incremental edge functions (exact: |E| < 2^30 for extents <= 64 px).  The
 // bbox is walked as one flat loop of w*h steps, so a warp runs max(w*h) steps over
@@ -663,7 +683,7 @@ __global__ void __launch_bounds__(256, 4) k_raster(Geo g, Batch b, const float* 
     uint32_t* ctr = count ? s_cnt : nullptr;
     if (threadIdx.x < 8) s_cnt[threadIdx.x] = 0;
     for (int j = threadIdx.x; j < TILE * TILE; j += blockDim.x) key[j] = ~0ull;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31;
     __syncthreads();
     if (valid) {
         const FaceInfo& F = g.face[bi.face];
@@ -735,7 +755,7 @@ __global__ void __launch_bounds__(256, 4) k_raster(Geo g, Batch b, const float* 
                 const short4 bx = s_box[i];
                 raster_small<TILE>(s_tri[i], bx.x, bx.y, bx.z, bx.w, bi, sx, sy, key);
             }
-            for (int i = warp; i < nbig; i += nwarp) {
+            for (int i = (int)(threadIdx.x >> 5); i < nbig; i += (int)(blockDim.x >> 5)) {
                 const RTri t = s_tri[s_bigi[i]];
                 const int32_t xmn = min(t.X[0], min(t.X[1], t.X[2])), xmx = max(t.X[0], max(t.X[1], t.X[2]));
                 const int32_t ymn = min(t.Y[0], min(t.Y[1], t.Y[2])), ymx = max(t.Y[0], max(t.Y[1], t.Y[2]));
@@ -755,66 +775,53 @@ __global__ void __launch_bounds__(256, 4) k_raster(Geo g, Batch b, const float* 
         if (v) atomicAdd(&st->raster_counters[threadIdx.x], (unsigned long long)v);
     }
     const size_t img = (size_t)hi * g.RES;
+    if (write_items)
+        for (int j = threadIdx.x; j < TILE * TILE; j += blockDim.x) {
+            const int ly = j / TILE, lx = j % TILE;
+            if (lx >= bi.w || ly >= bi.h) continue;
+            const unsigned long long k = key[j];
+            const bool has = valid && k != ~0ull;
+            b.items[img + (size_t)(bi.y0 + ly) * g.TW + bi.x0 + lx] = has ? (uint32_t)k + 1u : 0u;
+        }
+    if (!fused) return;
     uint32_t* h_id = reinterpret_cast<uint32_t*>(s_region);
     unsigned long long* h_sum = reinterpret_cast<unsigned long long*>(s_region + 4 * kHashSlots);
-    if (fused) {
-        for (int j = threadIdx.x; j < kHashSlots; j += blockDim.x) {
-            h_id[j] = kHashEmpty;
-            h_sum[j] = 0;
-        }
-        __syncthreads();
+    for (int j = threadIdx.x; j < kHashSlots; j += blockDim.x) {
+        h_id[j] = kHashEmpty;
+        h_sum[j] = 0;
     }
+    __syncthreads();
     unsigned long long* Fq = b.Fq + (size_t)hi * g.n;
-    for (int j = threadIdx.x; j < TILE * TILE; j += blockDim.x) {
-        const int ly = j / TILE, lx = j % TILE;
-        const bool inb = lx < bi.w && ly < bi.h;
-        const int px = bi.x0 + lx, py = bi.y0 + ly;
-        const unsigned long long k = key[j];
-        const bool has = inb && valid && k != ~0ull;
-        const uint32_t id = has ? (uint32_t)(k & 0xFFFFFFFFull) : 0xFFFFFFFFu;
-        if (write_items && inb) b.items[img + (size_t)py * g.TW + px] = has ? id + 1 : 0u;
-        if (fused) {
-            unsigned long long q = 0;
-            if (has) q = __float2ull_rz(fftab[(size_t)py * g.TW + px] * 0x1p61f);
-            // runs of equal ids over consecutive lanes: exact sum per run with redux.sync
-            const uint32_t prev = __shfl_up_sync(0xffffffffu, id, 1);
-            const bool head = lane == 0 || prev != id;
-            const unsigned heads = __ballot_sync(0xffffffffu, head);
-            const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
-            const int h = 31 - __clz(heads & upto);
-            const unsigned above = heads & ~upto;
-            const unsigned hi_mask = above ? ((1u << (__ffs(above) - 1)) - 1u) : 0xffffffffu;
-            const unsigned seg = hi_mask & ~((1u << h) - 1u);
-            const uint32_t a = (uint32_t)(q & 0x1FFFFFull), bb = (uint32_t)((q >> 21) & 0x1FFFFFull),
-                           c = (uint32_t)(q >> 42);
-            const uint32_t sa = __reduce_add_sync(seg, a), sb = __reduce_add_sync(seg, bb), sc = __reduce_add_sync(seg, c);
-            if (has && lane == h) {
-                const unsigned long long sum =
-                    (unsigned long long)sa + ((unsigned long long)sb << 21) + ((unsigned long long)sc << 42);
-                uint32_t slot = (id * 2654435761u) >> 22;
-                bool done = false;
-                for (int probe = 0; probe < 32 && !done; probe++) {
-                    uint32_t cur = h_id[slot];
-                    if (cur == kHashEmpty) {
-                        cur = atomicCAS(&h_id[slot], kHashEmpty, id);
-                        if (cur == kHashEmpty) cur = id;
-                    }
-                    if (cur == id) {
-                        atomicAdd(&h_sum[slot], sum);
-                        done = true;
-                    }
-                    slot = (slot + 1) & (kHashSlots - 1);
-                }
-                if (!done) atomicAdd(&Fq[id], sum);  // table crowded: straight to the global sum
+    // Each thread walks kSeg consecutive pixels down one column of the bin, summing the
+    // exact fixed-point delta form factors (ff * 2^61) while the patch id stays the same,
+    // and adds each run's sum to the bin's id -> sum table once.  Lanes take adjacent
+    // columns, so key and table reads are conflict-free / coalesced.
+    constexpr int kSeg = TILE * TILE / 256 > 4 ? TILE * TILE / 256 : 4;
+    constexpr int kWalkers = TILE * TILE / kSeg;
+    if (valid && (int)threadIdx.x < kWalkers) {
+        const int x = threadIdx.x % TILE, r0 = (threadIdx.x / TILE) * kSeg;
+        const bool col_in = x < bi.w;
+        const float* ffcol = fftab + (size_t)(bi.y0 + r0) * g.TW + bi.x0 + x;
+        uint32_t cur = kHashEmpty;
+        unsigned long long acc = 0;
+#pragma unroll 8
+        for (int i = 0; i < kSeg; i++) {
+            const unsigned long long k = key[(r0 + i) * TILE + x];
+            const bool has = col_in && r0 + i < bi.h && k != ~0ull;
+            const uint32_t id = has ? (uint32_t)k : kHashEmpty;
+            if (id != cur) {
+                if (cur != kHashEmpty) hash_add(h_id, h_sum, Fq, cur, acc);
+                cur = id;
+                acc = 0;
             }
+            if (has) acc += __float2ull_rz(ffcol[(size_t)i * g.TW] * 0x1p61f);
         }
+        if (cur != kHashEmpty) hash_add(h_id, h_sum, Fq, cur, acc);
     }
-    if (fused) {
-        __syncthreads();
-        for (int j = threadIdx.x; j < kHashSlots; j += blockDim.x) {
-            const uint32_t id = h_id[j];
-            if (id != kHashEmpty) atomicAdd(&Fq[id], h_sum[j]);
-        }
+    __syncthreads();
+    for (int j = threadIdx.x; j < kHashSlots; j += blockDim.x) {
+        const uint32_t id = h_id[j];
+        if (id != kHashEmpty) atomicAdd(&Fq[id], h_sum[j]);
     }
 }
 
