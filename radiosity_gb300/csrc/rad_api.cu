@@ -96,6 +96,7 @@ static void free_batch(BatchBuf& bb) {
     dfree(bb.b.frame);
     dfree(bb.b.tris);
     dfree(bb.b.bin_count);
+    dfree(bb.b.tri_counts);
     dfree(bb.b.bin_offset);
     dfree(bb.b.bin_fill);
     dfree(bb.b.bin_list);
@@ -130,6 +131,7 @@ static int alloc_batch(rad_ctx* c, BatchBuf& bb, uint32_t K, bool items) {
         return fail(c, RAD_E_INVALID, "batch capacity exceeds 2^32 records; lower hemicubes_count");
     b.K = K;
     b.tri_cap = (uint32_t)tri_cap;
+    b.tri_cap_h = tri_cap_per_hemi(c);
     b.list_cap = (uint32_t)list_cap;
     const size_t nbk = (size_t)K * c->geo.nb;
     RAD_CUDA(c, cudaMalloc(&b.shooters, sizeof(uint32_t) * K));
@@ -139,6 +141,7 @@ static int alloc_batch(rad_ctx* c, BatchBuf& bb, uint32_t K, bool items) {
     RAD_CUDA(c, cudaMalloc(&b.frame, sizeof(float) * 8 * K));
     RAD_CUDA(c, cudaMalloc(&b.tris, sizeof(TriRec) * tri_cap));
     RAD_CUDA(c, cudaMalloc(&b.bin_count, sizeof(uint32_t) * nbk));
+    RAD_CUDA(c, cudaMalloc(&b.tri_counts, sizeof(uint32_t) * K));
     RAD_CUDA(c, cudaMalloc(&b.bin_offset, sizeof(uint32_t) * nbk));
     RAD_CUDA(c, cudaMalloc(&b.bin_fill, sizeof(uint32_t) * nbk));
     RAD_CUDA(c, cudaMalloc(&b.bin_list, sizeof(uint32_t) * list_cap));
@@ -178,6 +181,7 @@ static void setup_geo(rad_ctx* c, std::vector<BinInfo>& bins) {
     if (tile == 0) tile = W >= 512 ? 64 : (W >= 64 ? 32 : 16);
     g.tile = tile;
     g.small_max = c->cfg.small_tri_pixels ? c->cfg.small_tri_pixels : 64;
+    g.piece = std::max(32u, (g.small_max + 7u) / 8u);  // at most 8 pieces per small triangle
     const int w = (int)W, h = (int)W;
     uint32_t base = 0;
     bins.clear();
@@ -251,7 +255,7 @@ static int check_cfg(const rad_config* cfg) {
 static void enqueue_batch(rad_ctx* c) {
     Batch& b = c->shoot.b;
     cudaStream_t s = c->stream;
-    cudaMemsetAsync(&c->d_state->tri_count, 0, sizeof(uint32_t), s);
+    cudaMemsetAsync(b.tri_counts, 0, sizeof(uint32_t) * b.K, s);
     cudaMemsetAsync(b.bin_count, 0, sizeof(uint32_t) * (size_t)b.K * c->geo.nb, s);
     launch_select(c->geo, b, c->d_rad, c->d_area, c->d_state, s);
     launch_camera(c->geo, b, c->d_verts, c->d_rad, c->d_state, s);
@@ -277,6 +281,7 @@ static int run_aux(rad_ctx* c, const uint32_t* shooters, uint32_t count, bool it
     RAD_CUDA(c, cudaMemsetAsync(c->d_aux, 0, sizeof(DevState), s));
     RAD_CUDA(c, cudaMemcpyAsync(b.shooters, shooters, sizeof(uint32_t) * count, cudaMemcpyHostToDevice, s));
     RAD_CUDA(c, cudaMemcpyAsync(b.valid, ones.data(), sizeof(uint32_t) * count, cudaMemcpyHostToDevice, s));
+    RAD_CUDA(c, cudaMemsetAsync(b.tri_counts, 0, sizeof(uint32_t) * count, s));
     RAD_CUDA(c, cudaMemsetAsync(b.bin_count, 0, sizeof(uint32_t) * (size_t)count * c->geo.nb, s));
     RAD_CUDA(c, cudaMemsetAsync(b.Fq, 0, sizeof(unsigned long long) * (size_t)count * c->n, s));
     launch_camera(c->geo, b, c->d_verts, c->d_rad, c->d_aux, s);
@@ -598,7 +603,7 @@ int rad_profile_stages(rad_ctx* c, uint32_t n_shots, double* stage_ms, rad_stats
     float total_ms = 0;
     RAD_CUDA(c, cudaMemsetAsync(c->d_state->raster_counters, 0, sizeof(c->d_state->raster_counters), s));
     for (uint32_t shot = 0; shot < n_shots; shot++) {
-        RAD_CUDA(c, cudaMemsetAsync(&c->d_state->tri_count, 0, sizeof(uint32_t), s));
+        RAD_CUDA(c, cudaMemsetAsync(b.tri_counts, 0, sizeof(uint32_t) * b.K, s));
         RAD_CUDA(c, cudaMemsetAsync(b.bin_count, 0, sizeof(uint32_t) * (size_t)b.K * c->geo.nb, s));
         RAD_CUDA(c, cudaEventRecord(ev[0], s));
         launch_select(c->geo, b, c->d_rad, c->d_area, c->d_state, s);
@@ -674,6 +679,7 @@ static int time_pipeline(rad_ctx* c, const std::vector<uint32_t>& sh, int reps, 
     *best_ms = 1e30f;
     for (int r = 0; r < reps + 1; r++) {
         RAD_CUDA(c, cudaMemsetAsync(c->d_aux, 0, sizeof(DevState), s));
+        RAD_CUDA(c, cudaMemsetAsync(b.tri_counts, 0, sizeof(uint32_t) * count, s));
         RAD_CUDA(c, cudaMemsetAsync(b.bin_count, 0, sizeof(uint32_t) * (size_t)count * c->geo.nb, s));
         RAD_CUDA(c, cudaEventRecord(c->ev0, s));
         launch_camera(c->geo, b, c->d_verts, c->d_rad, c->d_aux, s);

@@ -51,7 +51,8 @@ struct Geo {
     uint32_t tile;             // bin side
     uint32_t mode;             // rad_mode
     uint32_t small_max;        // lane-mode threshold (clamped bbox pixels)
-    uint32_t pad0[3];
+    uint32_t piece;            // box pixels per lane piece of a small triangle, >= small_max / 8
+    uint32_t pad0[2];
     FaceInfo face[5];
     float proj[16];            // Perspective(90,1,0.01,1000), column-major
 };
@@ -61,7 +62,7 @@ struct DevState {
     uint32_t stopped;
     uint32_t shots_done;
     uint32_t overflow;
-    uint32_t tri_count;
+    uint32_t reserved;
     float last_energy[4];
     double residual;
     double power0;
@@ -76,15 +77,16 @@ struct DevState {
 // Device pointers of one batch of K hemicubes.
 struct Batch {
     uint32_t K;
-    uint32_t tri_cap;
+    uint32_t tri_cap;            // K * tri_cap_h
     uint32_t list_cap;
-    uint32_t pad;
+    uint32_t tri_cap_h;          // triangle records per hemicube
+    uint32_t* tri_counts;        // K per-hemicube record counts
     uint32_t* shooters;          // K
     uint32_t* valid;             // K
     float4* saved;               // K
     float* mvp;                  // K*5*16
     float* frame;                // K*8 (center xyz, normal xyz)
-    TriRec* tris;                // tri_cap
+    TriRec* tris;                // tri_cap: hemicube h owns [h*tri_cap_h, (h+1)*tri_cap_h)
     uint32_t* bin_count;         // K*nb
     uint32_t* bin_offset;        // K*nb
     uint32_t* bin_fill;          // K*nb

@@ -22,6 +22,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "camera.cuh"
 #include "rad_internal.cuh"
 
@@ -280,18 +282,19 @@ __device__ __noinline__ void emit_polygon(const Geo& g, const Batch& b, const fl
     SV sv[12];
     bool good = true;
     for (int k = 0; k < pn; k++) good = good && snap_vertex(poly[k], hw, hh, vx, vy, sv[k]);
+    TriRec* tris = b.tris + (size_t)hi * b.tri_cap_h;  // this hemicube's records
     for (int j = 0; j + 2 < pn; j++) {
         const uint32_t slot = base + (uint32_t)j;
-        if (slot >= b.tri_cap) {
+        if (slot >= b.tri_cap_h) {
             atomicOr(&st->overflow, 1u);
             return;
         }
         int px[4];
         if (good && tri_bbox(sv[0], sv[j + 1], sv[j + 2], F, px)) {
-            tri_write(sv[0], sv[j + 1], sv[j + 2], p, hi * 5 + (uint32_t)f, F, px, &b.tris[slot]);
+            tri_write(sv[0], sv[j + 1], sv[j + 2], p, hi * 5 + (uint32_t)f, F, px, &tris[slot]);
             count_bins(g, b, hi, F, px);
         } else {
-            b.tris[slot].id = kDeadTri;
+            tris[slot].id = kDeadTri;
         }
     }
 }
@@ -380,11 +383,12 @@ __global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* _
                 pn = clip_polygon(poly, 3);
             }
             const uint32_t ncand = fast ? (ok ? 1u : 0u) : (pn >= 3 ? (uint32_t)(pn - 2) : 0u);
-            const uint32_t base = warp_alloc(&st->tri_count, ncand);
-            const bool written = fast && ok && base < b.tri_cap;
+            // slots are allocated per hemicube (one counter each, not one for the batch)
+            const uint32_t base = warp_alloc(&b.tri_counts[hi], ncand);
+            const bool written = fast && ok && base < b.tri_cap_h;
             if (fast && ok) {
-                if (base >= b.tri_cap) atomicOr(&st->overflow, 1u);
-                else tri_write(s0, s1, s2, p, hi * 5 + (uint32_t)f, F, px, &b.tris[base]);
+                if (base >= b.tri_cap_h) atomicOr(&st->overflow, 1u);
+                else tri_write(s0, s1, s2, p, hi * 5 + (uint32_t)f, F, px, &b.tris[(size_t)hi * b.tri_cap_h + base]);
             } else if (ncand) {
                 emit_polygon(g, b, poly, pn, base, p, hi, f, hw, hh, vx, vy, st);
             }
@@ -429,22 +433,25 @@ __global__ void __launch_bounds__(1024) k_scan(Geo g, Batch b, DevState* st) {
 
 __global__ void k_fill(Geo g, Batch b, DevState* st) {
     if (st->stopped) return;
-    const uint32_t ntri = min(st->tri_count, b.tri_cap);
+    const uint32_t hi = blockIdx.y;
+    const uint32_t ntri = min(b.tri_counts[hi], b.tri_cap_h);
+    const TriRec* tris = b.tris + (size_t)hi * b.tri_cap_h;
     const int tile = (int)g.tile;
     const uint32_t lane = threadIdx.x & 31;
     // warp-uniform trip count so that single-bin triangles can be grouped by bin
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t s0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); s0 < ntri; s0 += stride) {
         const uint32_t s = s0 + lane;
+        const uint32_t gs = hi * b.tri_cap_h + s;  // batch-wide record index
         bool on = s < ntri;
         int c0 = 0, c1 = -1, r0 = 0, r1 = -1;
         size_t gb0 = 0;
         uint32_t bins_x = 0;
         if (on) {
-            const TriRec& t = b.tris[s];
+            const TriRec& t = tris[s];
             on = t.id != kDeadTri;
             if (on) {
-                const uint32_t hi = t.hf / 5, f = t.hf % 5;
+                const uint32_t f = t.hf % 5;
                 const FaceInfo& F = g.face[f];
                 c0 = (t.px0 - F.sc[0]) / tile;
                 c1 = (t.px1 - F.sc[0]) / tile;
@@ -464,14 +471,14 @@ __global__ void k_fill(Geo g, Batch b, DevState* st) {
             if ((int)lane == leader) pos = atomicAdd(&b.bin_fill[gb1], (uint32_t)__popc(grp));
             pos = __shfl_sync(grp, pos, leader) + __popc(grp & ((1u << lane) - 1u));
             const uint32_t idx = b.bin_offset[gb1] + pos;
-            if (idx < b.list_cap) b.bin_list[idx] = s;
+            if (idx < b.list_cap) b.bin_list[idx] = gs;
         } else if (on) {
             for (int r = r0; r <= r1; r++)
                 for (int c = c0; c <= c1; c++) {
                     const size_t gb = gb0 + (size_t)r * bins_x + c;
                     const uint32_t pos = atomicAdd(&b.bin_fill[gb], 1u);
                     const uint32_t idx = b.bin_offset[gb] + pos;
-                    if (idx < b.list_cap) b.bin_list[idx] = s;
+                    if (idx < b.list_cap) b.bin_list[idx] = gs;
                 }
         }
     }
@@ -479,7 +486,7 @@ __global__ void k_fill(Geo g, Batch b, DevState* st) {
 
 void launch_bins(const Geo& g, const Batch& b, DevState* st, cudaStream_t s) {
     k_scan<<<1, 1024, 0, s>>>(g, b, st);
-    k_fill<<<152 * 8, 256, 0, s>>>(g, b, st);
+    k_fill<<<dim3(std::max(2u, (152u * 16u) / b.K), b.K), 256, 0, s>>>(g, b, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -508,6 +515,7 @@ constexpr int kHashSlots = 1024;     // per-bin id -> sum table of the reduction
 constexpr uint32_t kHashEmpty = 0xFFFFFFFFu;
 constexpr int kRegionBytes = 12 * kHashSlots;  // >= kChunk * (sizeof(RTri) + 8) (12 KB)
 constexpr int kSizeClasses = 16;               // ceil(log2(box pixels)) for boxes <= 2^15 px
+constexpr int kMaxPieces = 8;                  // pieces per small triangle (g.piece >= small_max / 8)
 
 // The parts of a triangle record the per-pixel loops need (40 bytes in shared memory).
 struct RTri {
@@ -520,6 +528,31 @@ static_assert(kChunk <= 256, "chunk indices are stored as uint8");
 
 __device__ __forceinline__ bool inside_edge(long long e, bool tl) { return e > 0 || (e == 0 && tl); }
 __device__ __forceinline__ bool inside_edge32(int32_t e, bool tl) { return e > 0 || (e == 0 && tl); }
+
+// Exclusive prefix sum of v over a 256-thread block; returns this thread's offset and
+// leaves the block total in ws[8].  Contains two __syncthreads.
+__device__ __forceinline__ int block_exclusive_scan(int v, uint32_t* ws) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[warp] = (uint32_t)x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int k = 0; k < 8; k++) {
+            const uint32_t t = ws[k];
+            ws[k] = run;
+            run += t;
+        }
+        ws[8] = run;
+    }
+    __syncthreads();
+    return (int)ws[warp] + x - v;
+}
 
 // Adds an exact partial sum to the bin's open-addressing id -> sum table (linear probing,
 // at most 32 probes); a crowded table sends the sum straight to the global row.
@@ -541,32 +574,32 @@ __device__ __forceinline__ void hash_add(uint32_t* h_id, unsigned long long* h_s
     atomicAdd(&Fq[id], sum);
 }
 
-// One lane rasterises a small triangle over its clamped bbox [x0,x1]x[y0,y1] with
-// 32-bit incremental edge functions (exact: |E| < 2^30 for extents <= 64 px).  The
-// bbox is walked as one flat loop of w*h steps, so a warp runs max(w*h) steps over
-// its lanes (a nested row/column loop would run about max(h) * max(w)).
+// One lane rasterises pixels [start, start + steps) of a small triangle's clamped bbox
+// [x0,x1]x[y0,y1] (row-major flat order) with 32-bit incremental edge functions (exact:
+// |E| < 2^30 for extents <= 64 px), one flat loop of `steps` iterations.
 template <int TILE>
-__device__ __forceinline__ void raster_small(const RTri& t, int x0, int x1, int y0, int y1, const BinInfo& bi, int sx,
-                                             int sy, unsigned long long* key) {
+__device__ __forceinline__ void raster_small(const RTri& t, int x0, int x1, int y0, int start, int steps,
+                                             const BinInfo& bi, int sx, int sy, unsigned long long* key) {
+    const int w = x1 - x0 + 1;
+    const int ry = start / w, rx = start - ry * w;
+    int px = x0 + rx, py = y0 + ry;
     int32_t er[3], e[3], stx[3], sty[3];
     bool tl[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         const int j = k == 2 ? 0 : k + 1;
         const int32_t dx = t.X[j] - t.X[k], dy = t.Y[j] - t.Y[k];
-        er[k] = dx * (y0 * 256 + 128 - t.Y[k]) - dy * (x0 * 256 + 128 - t.X[k]);
-        e[k] = er[k];
+        er[k] = dx * (py * 256 + 128 - t.Y[k]) - dy * (x0 * 256 + 128 - t.X[k]);
         stx[k] = -dy * 256;
         sty[k] = dx * 256;
+        e[k] = er[k] + stx[k] * rx;
         tl[k] = (t.Y[j] < t.Y[k]) || (t.Y[j] == t.Y[k] && t.X[j] < t.X[k]);
     }
-    const int steps = (x1 - x0 + 1) * (y1 - y0 + 1);
-    int px = x0, py = y0;
     int row = (py - bi.y0) * TILE - (int)bi.x0;  // key index of pixel (px, py) = row + px
     for (int i = 0; i < steps; i++) {
         if (inside_edge32(e[0], tl[0]) && inside_edge32(e[1], tl[1]) && inside_edge32(e[2], tl[2])) {
-            const float u = (float)(px - sx), w = (float)(py - sy);
-            const float D = (t.c0 + t.ax * u) + t.ay * w;
+            const float u = (float)(px - sx), wv = (float)(py - sy);
+            const float D = (t.c0 + t.ax * u) + t.ay * wv;
             atomicMin(&key[row + px], ((unsigned long long)depth_ordinal(D) << 32) | t.id);
         }
         if (px < x1) {
@@ -633,22 +666,38 @@ __device__ __forceinline__ void raster_big(const RTri& t, int x0, int x1, int y0
         const unsigned lm = __ballot_sync(0xffffffffu, live), am = __ballot_sync(0xffffffffu, live && acc);
         visited += __popc(lm);
         accepted += __popc(am);
+        // live stamps two at a time: the two pixel tests of a lane are independent
         unsigned todo = lm;
         while (todo) {
-            const int j = __ffs(todo) - 1;
+            const int j1 = __ffs(todo) - 1;
             todo &= todo - 1;
-            const int px = x0 + __shfl_sync(0xffffffffu, mcx, j) + lx, py = y0 + __shfl_sync(0xffffffffu, mcy, j) + ly;
-            const long long e0 = __shfl_sync(0xffffffffu, es[0], j), e1 = __shfl_sync(0xffffffffu, es[1], j),
-                            e2 = __shfl_sync(0xffffffffu, es[2], j);
-            bool in = px <= x1 && py <= y1;
-            if (in && !((am >> j) & 1u))
-                in = inside_edge(e0 + off[0], tl[0]) && inside_edge(e1 + off[1], tl[1]) &&
-                     inside_edge(e2 + off[2], tl[2]);
-            if (in) {
-                const float u = (float)(px - sx), w = (float)(py - sy);
+            const int j2 = todo ? __ffs(todo) - 1 : j1;
+            const bool two = todo != 0;
+            todo &= todo - 1;
+            const int pxa = x0 + __shfl_sync(0xffffffffu, mcx, j1) + lx, pya = y0 + __shfl_sync(0xffffffffu, mcy, j1) + ly;
+            const int pxb = x0 + __shfl_sync(0xffffffffu, mcx, j2) + lx, pyb = y0 + __shfl_sync(0xffffffffu, mcy, j2) + ly;
+            const long long a0 = __shfl_sync(0xffffffffu, es[0], j1), a1 = __shfl_sync(0xffffffffu, es[1], j1),
+                            a2 = __shfl_sync(0xffffffffu, es[2], j1);
+            const long long b0 = __shfl_sync(0xffffffffu, es[0], j2), b1 = __shfl_sync(0xffffffffu, es[1], j2),
+                            b2 = __shfl_sync(0xffffffffu, es[2], j2);
+            bool ina = pxa <= x1 && pya <= y1;
+            bool inb = two && pxb <= x1 && pyb <= y1;
+            if (ina && !((am >> j1) & 1u))
+                ina = inside_edge(a0 + off[0], tl[0]) && inside_edge(a1 + off[1], tl[1]) &&
+                      inside_edge(a2 + off[2], tl[2]);
+            if (inb && !((am >> j2) & 1u))
+                inb = inside_edge(b0 + off[0], tl[0]) && inside_edge(b1 + off[1], tl[1]) &&
+                      inside_edge(b2 + off[2], tl[2]);
+            if (ina) {
+                const float u = (float)(pxa - sx), w = (float)(pya - sy);
                 const float D = (t.c0 + t.ax * u) + t.ay * w;
-                const unsigned long long k = ((unsigned long long)depth_ordinal(D) << 32) | t.id;
-                atomicMin(&key[(py - bi.y0) * TILE + (px - bi.x0)], k);
+                atomicMin(&key[(pya - bi.y0) * TILE + (pxa - bi.x0)], ((unsigned long long)depth_ordinal(D) << 32) | t.id);
+                plotted++;
+            }
+            if (inb) {
+                const float u = (float)(pxb - sx), w = (float)(pyb - sy);
+                const float D = (t.c0 + t.ax * u) + t.ay * w;
+                atomicMin(&key[(pyb - bi.y0) * TILE + (pxb - bi.x0)], ((unsigned long long)depth_ordinal(D) << 32) | t.id);
                 plotted++;
             }
         }
@@ -678,6 +727,9 @@ __global__ void __launch_bounds__(256, 4) k_raster(Geo g, Batch b, const float* 
     __shared__ uint8_t s_order[kChunk];  // small triangles by size class (ascending)
     __shared__ uint8_t s_bigi[kChunk];   // big triangles
     __shared__ uint32_t s_ncls[kSizeClasses];
+    __shared__ uint16_t s_poff[kChunk];                 // first piece of each sorted small triangle
+    __shared__ uint8_t s_owner[kChunk * kMaxPieces];    // piece -> sorted position
+    __shared__ uint32_t s_wsum[9];
     __shared__ int s_nbig, s_nsmall;
     __shared__ uint32_t s_cnt[8];
     uint32_t* ctr = count ? s_cnt : nullptr;
@@ -747,13 +799,30 @@ __global__ void __launch_bounds__(256, 4) k_raster(Geo g, Batch b, const float* 
             __syncthreads();
             if (cls >= 0) s_order[s_ncls[cls] + rank] = (uint8_t)threadIdx.x;
             __syncthreads();
-            // 3. small triangles, one per lane, in size order: a warp's lanes walk boxes of
-            //    similar size; then big triangles, one per warp (no barrier between)
+            // 3. small triangles in size order, each cut into L <= kMaxPieces equal pieces of
+            //    at most g.piece box pixels, one piece per lane: lanes and warps get similar
+            //    amounts of work; then big triangles, one per warp (no barrier between)
             const int nsmall = s_nsmall, nbig = s_nbig;
+            int np = 0;
             if ((int)threadIdx.x < nsmall) {
-                const int i = s_order[threadIdx.x];
+                const short4 bx = s_box[s_order[threadIdx.x]];
+                const int area = (bx.y - bx.x + 1) * (bx.w - bx.z + 1);
+                np = (area + (int)g.piece - 1) / (int)g.piece;
+            }
+            const int poff = block_exclusive_scan(np, s_wsum);  // syncs; s_wsum[8] = total
+            if (np) {
+                s_poff[threadIdx.x] = (uint16_t)poff;
+                for (int j = 0; j < np; j++) s_owner[poff + j] = (uint8_t)threadIdx.x;
+            }
+            __syncthreads();
+            const int npieces = (int)s_wsum[8];
+            for (int gp = threadIdx.x; gp < npieces; gp += blockDim.x) {
+                const int pos = s_owner[gp], i = s_order[pos];
                 const short4 bx = s_box[i];
-                raster_small<TILE>(s_tri[i], bx.x, bx.y, bx.z, bx.w, bi, sx, sy, key);
+                const int w = bx.y - bx.x + 1, area = w * (bx.w - bx.z + 1);
+                const int L = (area + (int)g.piece - 1) / (int)g.piece, per = (area + L - 1) / L;
+                const int start = (gp - (int)s_poff[pos]) * per;
+                raster_small<TILE>(s_tri[i], bx.x, bx.y, bx.z, start, min(per, area - start), bi, sx, sy, key);
             }
             for (int i = (int)(threadIdx.x >> 5); i < nbig; i += (int)(blockDim.x >> 5)) {
                 const RTri t = s_tri[s_bigi[i]];
