@@ -180,6 +180,8 @@ static void setup_geo(rad_ctx* c, std::vector<BinInfo>& bins) {
     uint32_t tile = c->cfg.tile;
     if (tile == 0) tile = W >= 512 ? 64 : (W >= 64 ? 32 : 16);
     g.tile = tile;
+    g.tile_shift = 0;
+    while ((1u << g.tile_shift) < tile) g.tile_shift++;
     g.small_max = c->cfg.small_tri_pixels ? c->cfg.small_tri_pixels : 64;
     g.piece = std::max(32u, (g.small_max + 7u) / 8u);  // at most 8 pieces per small triangle
     const int w = (int)W, h = (int)W;

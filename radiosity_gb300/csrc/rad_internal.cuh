@@ -52,7 +52,8 @@ struct Geo {
     uint32_t mode;             // rad_mode
     uint32_t small_max;        // lane-mode threshold (clamped bbox pixels)
     uint32_t piece;            // box pixels per lane piece of a small triangle, >= small_max / 8
-    uint32_t pad0[2];
+    uint32_t tile_shift;       // log2(tile)
+    uint32_t pad0;
     FaceInfo face[5];
     float proj[16];            // Perspective(90,1,0.01,1000), column-major
 };

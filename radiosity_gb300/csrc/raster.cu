@@ -230,12 +230,13 @@ __device__ __forceinline__ void tri_write(SV a, SV b, SV c, uint32_t id, uint32_
     o[3] = make_int4((int)hf, 0, 0, 0);
 }
 
-__device__ __forceinline__ void count_bins(const Geo& g, const Batch& b, uint32_t hi, const FaceInfo& F,
-                                           const int* px) {
-    const int tile = (int)g.tile;
-    int c0 = (px[0] - F.sc[0]) / tile, c1 = (px[1] - F.sc[0]) / tile;
-    int r0 = (px[2] - F.sc[1]) / tile, r1 = (px[3] - F.sc[1]) / tile;
-    uint32_t* cnt = b.bin_count + (size_t)hi * g.nb + F.bin_base;
+// Adds one to each bin the pixel box px touches; cnt = the hemicube's bin counters
+// (the CTA's shared-memory histogram or the global counts).
+__device__ __forceinline__ void count_bins(const Geo& g, const FaceInfo& F, const int* px, uint32_t* cnt) {
+    const int sh = (int)g.tile_shift;  // boxes lie inside the scissor: offsets are >= 0
+    const int c0 = (px[0] - F.sc[0]) >> sh, c1 = (px[1] - F.sc[0]) >> sh;
+    const int r0 = (px[2] - F.sc[1]) >> sh, r1 = (px[3] - F.sc[1]) >> sh;
+    cnt += F.bin_base;
     for (int r = r0; r <= r1; r++)
         for (int c = c0; c <= c1; c++) atomicAdd(&cnt[r * F.bins_x + c], 1u);
 }
@@ -245,13 +246,13 @@ __device__ __forceinline__ void count_bins(const Geo& g, const Batch& b, uint32_
 // with one atomic per group; the others count their bins one by one.
 __device__ __forceinline__ void count_bins_warp(const Geo& g, const Batch& b, uint32_t hi, const FaceInfo& F,
                                                 const int* px, bool on) {
-    const int tile = (int)g.tile;
+    const int sh = (int)g.tile_shift;
     int c0 = 0, c1 = -1, r0 = 0, r1 = -1;
     if (on) {
-        c0 = (px[0] - F.sc[0]) / tile;
-        c1 = (px[1] - F.sc[0]) / tile;
-        r0 = (px[2] - F.sc[1]) / tile;
-        r1 = (px[3] - F.sc[1]) / tile;
+        c0 = (px[0] - F.sc[0]) >> sh;
+        c1 = (px[1] - F.sc[0]) >> sh;
+        r0 = (px[2] - F.sc[1]) >> sh;
+        r1 = (px[3] - F.sc[1]) >> sh;
     }
     uint32_t* cnt = b.bin_count + (size_t)hi * g.nb + F.bin_base;
     const bool single = on && c0 == c1 && r0 == r1;
@@ -277,7 +278,7 @@ __device__ __forceinline__ bool snap_vertex(float4 c, float hw, float hh, float 
 // Fan triangles of a clipped polygon into slots base .. base+pn-3 (culled ones marked dead).
 __device__ __noinline__ void emit_polygon(const Geo& g, const Batch& b, const float4* poly, int pn, uint32_t base,
                                           uint32_t p, uint32_t hi, int f, float hw, float hh, float vx, float vy,
-                                          DevState* st) {
+                                          uint32_t* cnt, DevState* st) {
     const FaceInfo& F = g.face[f];
     SV sv[12];
     bool good = true;
@@ -292,80 +293,139 @@ __device__ __noinline__ void emit_polygon(const Geo& g, const Batch& b, const fl
         int px[4];
         if (good && tri_bbox(sv[0], sv[j + 1], sv[j + 2], F, px)) {
             tri_write(sv[0], sv[j + 1], sv[j + 2], p, hi * 5 + (uint32_t)f, F, px, &tris[slot]);
-            count_bins(g, b, hi, F, px);
+            count_bins(g, F, px, cnt);
         } else {
             tris[slot].id = kDeadTri;
         }
     }
 }
 
+// Clip-space corners of quad q (12 floats) under face f's MVP mm, and whether the quad
+// can cover a pixel of face f: not all corners outside one clip plane, and at least one
+// corner on the kept half of a side face (source/Main.cpp:349-389).
+__device__ __forceinline__ bool face_corners(const float* q, const float* mm, int f, float4* cv) {
+    uint32_t out_any = 0x3F, in_half = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const float x = q[3 * k], y = q[3 * k + 1], z = q[3 * k + 2];
+        float4 c;
+        c.x = ((mm[0] * x + mm[4] * y) + mm[8] * z) + mm[12];
+        c.y = ((mm[1] * x + mm[5] * y) + mm[9] * z) + mm[13];
+        c.z = ((mm[2] * x + mm[6] * y) + mm[10] * z) + mm[14];
+        c.w = ((mm[3] * x + mm[7] * y) + mm[11] * z) + mm[15];
+        cv[k] = c;
+        uint32_t o = 0;
+        if (c.z + c.w < 0) o |= 1;
+        if (c.w - c.z < 0) o |= 2;
+        if (c.x > c.w) o |= 4;
+        if (c.x < -c.w) o |= 8;
+        if (c.y > c.w) o |= 16;
+        if (c.y < -c.w) o |= 32;
+        out_any &= o;
+        bool keep = true;
+        if (f == 0) keep = c.y < 0;        // UP keeps y_ndc < 0
+        else if (f == 1) keep = c.y > 0;   // DOWN keeps y_ndc > 0
+        else if (f == 2) keep = c.x > 0;   // LEFT keeps x_ndc > 0
+        else if (f == 3) keep = c.x < 0;   // RIGHT keeps x_ndc < 0
+        if (keep) in_half = 1;
+    }
+    return !out_any && in_half;
+}
+
+__device__ __forceinline__ void load_quad(const float* verts, uint32_t p, float* q) {
+    const float4* src = reinterpret_cast<const float4*>(verts + 12 * (size_t)p);
+    const float4 a = __ldg(src), bq = __ldg(src + 1), c = __ldg(src + 2);
+    q[0] = a.x; q[1] = a.y; q[2] = a.z; q[3] = a.w;
+    q[4] = bq.x; q[5] = bq.y; q[6] = bq.z; q[7] = bq.w;
+    q[8] = c.x; q[9] = c.y; q[10] = c.z; q[11] = c.w;
+}
+
+constexpr uint32_t kSetupHistBins = 4096;  // 16 KB of shared memory at most
+
+// Thread per (hemicube, patch) in three phases:
+//  1. tangent-plane cull and the exact per-face test -> a 5-bit mask of faces to draw;
+//  2. warp compaction of the (patch, face) items;
+//  3. the warp's items, one per lane with all lanes busy: corners again, clip or snap,
+//     records, bin counts.
 __global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* __restrict__ verts, DevState* st) {
     if (st->stopped) return;
     const uint32_t hi = blockIdx.y;
     if (!b.valid[hi]) return;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    bool active = p < g.n;
     __shared__ float s_mvp[5 * 16];
     __shared__ float s_fr[8];
+    __shared__ uint8_t s_items[4][32 * 5];  // (lane << 3) | face
+    // per-CTA bin histogram (when the hemicube has <= kSetupHistBins bins): shared-memory
+    // atomics per triangle, one global add per touched bin at the end
+    extern __shared__ uint32_t s_hist[];
+    const bool use_hist = g.nb <= kSetupHistBins;
+    uint32_t* gcnt = b.bin_count + (size_t)hi * g.nb;
+    uint32_t* cnt = use_hist ? s_hist : gcnt;
     for (int i = threadIdx.x; i < 5 * 16; i += blockDim.x) s_mvp[i] = b.mvp[(size_t)hi * 80 + i];
     if (threadIdx.x < 8) s_fr[threadIdx.x] = b.frame[(size_t)hi * 8 + threadIdx.x];
+    if (use_hist)
+        for (uint32_t i = threadIdx.x; i < g.nb; i += blockDim.x) s_hist[i] = 0;
     __syncthreads();
-    const float cx = s_fr[0], cy = s_fr[1], cz = s_fr[2], nx = s_fr[3], ny = s_fr[4], nz = s_fr[5];
-    float4 cv[4];
-    const float4* src = reinterpret_cast<const float4*>(verts + 12 * (size_t)(active ? p : 0));
-    if (active) {
-        const float4 a = __ldg(src), bq = __ldg(src + 1), c = __ldg(src + 2);
-        const float q[12] = {a.x, a.y, a.z, a.w, bq.x, bq.y, bq.z, bq.w, c.x, c.y, c.z, c.w};
+    // 1. cull + face mask
+    uint32_t mask = 0;
+    if (p < g.n) {
+        const float cx = s_fr[0], cy = s_fr[1], cz = s_fr[2], nx = s_fr[3], ny = s_fr[4], nz = s_fr[5];
+        float q[12];
+        load_quad(verts, p, q);
         bool behind = true;
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            float d = ((q[3 * k] - cx) * nx + (q[3 * k + 1] - cy) * ny) + (q[3 * k + 2] - cz) * nz;
+            const float d = ((q[3 * k] - cx) * nx + (q[3 * k + 1] - cy) * ny) + (q[3 * k + 2] - cz) * nz;
             if (!(d < 0)) behind = false;
         }
-        if (behind) active = false;
-    }
-    for (int f = 0; f < 5; f++) {
-        const FaceInfo& F = g.face[f];
-        bool fa = active;
-        if (fa) {
-            const float* mm = s_mvp + f * 16;
-            uint32_t out_any = 0x3F, in_half = 0;
-            const float4 qa = __ldg(src), qb = __ldg(src + 1), qc = __ldg(src + 2);
-            const float q[12] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w};
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                float x = q[3 * k], y = q[3 * k + 1], z = q[3 * k + 2];
-                float4 c;
-                c.x = ((mm[0] * x + mm[4] * y) + mm[8] * z) + mm[12];
-                c.y = ((mm[1] * x + mm[5] * y) + mm[9] * z) + mm[13];
-                c.z = ((mm[2] * x + mm[6] * y) + mm[10] * z) + mm[14];
-                c.w = ((mm[3] * x + mm[7] * y) + mm[11] * z) + mm[15];
-                cv[k] = c;
-                uint32_t o = 0;
-                if (c.z + c.w < 0) o |= 1;
-                if (c.w - c.z < 0) o |= 2;
-                if (c.x > c.w) o |= 4;
-                if (c.x < -c.w) o |= 8;
-                if (c.y > c.w) o |= 16;
-                if (c.y < -c.w) o |= 32;
-                out_any &= o;
-                // scissor half of the side faces (source/Main.cpp:349-389)
-                bool keep = true;
-                if (f == 0) keep = c.y < 0;        // UP keeps y_ndc < 0
-                else if (f == 1) keep = c.y > 0;   // DOWN keeps y_ndc > 0
-                else if (f == 2) keep = c.x > 0;   // LEFT keeps x_ndc > 0
-                else if (f == 3) keep = c.x < 0;   // RIGHT keeps x_ndc < 0
-                if (keep) in_half = 1;
+        if (!behind)
+            for (int f = 0; f < 5; f++) {
+                float4 cv[4];
+                if (face_corners(q, s_mvp + f * 16, f, cv)) mask |= 1u << f;
             }
-            if (out_any || !in_half) fa = false;
+    }
+    // 2. compaction
+    const uint32_t nmine = __popc(mask);
+    uint32_t incl = nmine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    uint8_t* items = s_items[warp];
+    {
+        uint32_t k = incl - nmine;
+        for (int f = 0; f < 5; f++)
+            if ((mask >> f) & 1u) items[k++] = (uint8_t)((lane << 3) | (uint32_t)f);
+    }
+    __syncwarp();
+    // 3. items, 32 at a time
+    const uint32_t pbase = blockIdx.x * blockDim.x + warp * 32;
+    for (uint32_t r = 0; r < total; r += 32) {
+        const bool has = r + lane < total;
+        uint32_t pp = 0;
+        int f = 0;
+        if (has) {
+            const uint32_t it = items[r + lane];
+            pp = pbase + (it >> 3);
+            f = (int)(it & 7u);
+        }
+        const FaceInfo& F = g.face[f];
+        float4 cv[4];
+        if (has) {
+            float q[12];
+            load_quad(verts, pp, q);
+            face_corners(q, s_mvp + f * 16, f, cv);
         }
         const float hw = 0.5f * (float)F.vp[2], hh = 0.5f * (float)F.vp[3];
         const float vx = (float)F.vp[0], vy = (float)F.vp[1];
 #pragma unroll
         for (int t = 0; t < 2; t++) {
             const float4 va = cv[0], vb = cv[1 + t], vc = cv[2 + t];
-            const bool clip = fa && (needs_clip(va) || needs_clip(vb) || needs_clip(vc));
-            const bool fast = fa && !clip;
+            const bool clip = has && (needs_clip(va) || needs_clip(vb) || needs_clip(vc));
+            const bool fast = has && !clip;
             SV s0, s1, s2;
             int px[4];
             bool ok = false;
@@ -388,18 +448,28 @@ __global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* _
             const bool written = fast && ok && base < b.tri_cap_h;
             if (fast && ok) {
                 if (base >= b.tri_cap_h) atomicOr(&st->overflow, 1u);
-                else tri_write(s0, s1, s2, p, hi * 5 + (uint32_t)f, F, px, &b.tris[(size_t)hi * b.tri_cap_h + base]);
+                else tri_write(s0, s1, s2, pp, hi * 5 + (uint32_t)f, F, px, &b.tris[(size_t)hi * b.tri_cap_h + base]);
             } else if (ncand) {
-                emit_polygon(g, b, poly, pn, base, p, hi, f, hw, hh, vx, vy, st);
+                emit_polygon(g, b, poly, pn, base, pp, hi, f, hw, hh, vx, vy, cnt, st);
             }
-            count_bins_warp(g, b, hi, F, px, written);
+            if (use_hist) {
+                if (written) count_bins(g, F, px, cnt);
+            } else {
+                count_bins_warp(g, b, hi, F, px, written);
+            }
         }
+    }
+    if (use_hist) {
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < g.nb; i += blockDim.x)
+            if (s_hist[i]) atomicAdd(&gcnt[i], s_hist[i]);
     }
 }
 
 void launch_setup(const Geo& g, const Batch& b, const float* verts, DevState* st, cudaStream_t s) {
     dim3 grid((g.n + 127) / 128, b.K);
-    k_setup<<<grid, 128, 0, s>>>(g, b, verts, st);
+    const size_t hist = g.nb <= kSetupHistBins ? sizeof(uint32_t) * g.nb : 0;
+    k_setup<<<grid, 128, hist, s>>>(g, b, verts, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -436,7 +506,7 @@ __global__ void k_fill(Geo g, Batch b, DevState* st) {
     const uint32_t hi = blockIdx.y;
     const uint32_t ntri = min(b.tri_counts[hi], b.tri_cap_h);
     const TriRec* tris = b.tris + (size_t)hi * b.tri_cap_h;
-    const int tile = (int)g.tile;
+    const int sh = (int)g.tile_shift;
     const uint32_t lane = threadIdx.x & 31;
     // warp-uniform trip count so that single-bin triangles can be grouped by bin
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -453,10 +523,10 @@ __global__ void k_fill(Geo g, Batch b, DevState* st) {
             if (on) {
                 const uint32_t f = t.hf % 5;
                 const FaceInfo& F = g.face[f];
-                c0 = (t.px0 - F.sc[0]) / tile;
-                c1 = (t.px1 - F.sc[0]) / tile;
-                r0 = (t.py0 - F.sc[1]) / tile;
-                r1 = (t.py1 - F.sc[1]) / tile;
+                c0 = (t.px0 - F.sc[0]) >> sh;
+                c1 = (t.px1 - F.sc[0]) >> sh;
+                r0 = (t.py0 - F.sc[1]) >> sh;
+                r1 = (t.py1 - F.sc[1]) >> sh;
                 gb0 = (size_t)hi * g.nb + F.bin_base;
                 bins_x = F.bins_x;
             }
