@@ -349,6 +349,7 @@ int rad_create(const rad_config* cfg, rad_ctx** out) {
         return code;
     };
     if (cudaSetDevice(cfg->device) != cudaSuccess) return bail(RAD_E_CUDA);
+    if (raster_init() != cudaSuccess) return bail(RAD_E_CUDA);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(RAD_E_CUDA);
     if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) return bail(RAD_E_CUDA);
     std::vector<BinInfo> bins;

@@ -21,16 +21,27 @@ constexpr float kReflectivity = 0.3f;   // REFLECTIVITY, source/Patch.h:13
 constexpr uint32_t kDeadTri = 0xFFFFFFFFu;
 constexpr int kMaxK = 1024;
 
-// One rasterisable triangle, hemicube-local 24.8 fixed-point window coordinates.
+// One rasterisable record: up to two triangles of one patch that share vertex 0,
+// A = (v0, v1, v2) and B = (v0, v2, v3).  An unclipped patch quad is one record (its
+// two triangles, source/ModelContainer.cpp:166-171); a clipped triangle's fan is
+// packed two triangles per record.  Hemicube-local 24.8 fixed-point window coordinates.
+// Each triangle keeps its own depth plane; the plane's constant term is rebuilt from
+// d0 exactly as it was computed: c0 = (d0 + gx*ox) + gy*oy with gx = ax / 256.
 struct __align__(16) TriRec {
-    int32_t X0, Y0, X1, Y1, X2, Y2;
-    float c0, ax, ay;       // depth (1/w) plane: D = (c0 + ax*(px-sx)) + ay*(py-sy)
+    int32_t X[4], Y[4];     // v3 = v2 when B is absent
+    float d0;               // 1/w at v0
+    float ax[2], ay[2];     // plane gradients x256 of A and B: D = (c0 + ax*(px-sx)) + ay*(py-sy)
     uint32_t id;            // patch index, kDeadTri for an unused slot
-    int16_t px0, px1, py0, py1;  // pixel bbox clamped to the face scissor
-    uint32_t hf;            // hi*5 + face
-    uint32_t pad[3];
+    uint32_t bx, by;        // union pixel bbox clamped to the face scissor:
+                            // bx = px0 | px1 << 12 | face << 24 | A << 28 | B << 29, by = py0 | py1 << 12
 };
 static_assert(sizeof(TriRec) == 64, "TriRec layout");
+constexpr uint32_t kRecA = 1u << 28, kRecB = 1u << 29;
+__host__ __device__ inline int rec_px0(const TriRec& t) { return (int)(t.bx & 0xFFFu); }
+__host__ __device__ inline int rec_px1(const TriRec& t) { return (int)((t.bx >> 12) & 0xFFFu); }
+__host__ __device__ inline int rec_face(const TriRec& t) { return (int)((t.bx >> 24) & 7u); }
+__host__ __device__ inline int rec_py0(const TriRec& t) { return (int)(t.by & 0xFFFu); }
+__host__ __device__ inline int rec_py1(const TriRec& t) { return (int)((t.by >> 12) & 0xFFFu); }
 
 struct BinInfo {
     int16_t x0, y0, w, h;   // hemicube-local pixel rectangle
@@ -87,7 +98,7 @@ struct Batch {
     float4* saved;               // K
     float* mvp;                  // K*5*16
     float* frame;                // K*8 (center xyz, normal xyz)
-    TriRec* tris;                // tri_cap: hemicube h owns [h*tri_cap_h, (h+1)*tri_cap_h)
+    TriRec* tris;                // tri_cap records: hemicube h owns [h*tri_cap_h, (h+1)*tri_cap_h)
     uint32_t* bin_count;         // K*nb
     uint32_t* bin_offset;        // K*nb
     uint32_t* bin_fill;          // K*nb
@@ -110,6 +121,7 @@ void launch_camera(const Geo& g, const Batch& b, const float* verts, const float
                    cudaStream_t s);
 void launch_setup(const Geo& g, const Batch& b, const float* verts, DevState* st, cudaStream_t s);
 void launch_bins(const Geo& g, const Batch& b, DevState* st, cudaStream_t s);
+cudaError_t raster_init();  // per device, before the first launch_raster (dynamic shared memory limits)
 void launch_raster(const Geo& g, const Batch& b, const float* fftab, DevState* st, bool write_items,
                    bool fused_reduce, cudaStream_t s, bool count = false);
 void launch_reduce_items(const Geo& g, const Batch& b, const float* fftab, uint32_t count, cudaStream_t s);

@@ -209,25 +209,56 @@ __device__ __forceinline__ bool tri_bbox(SV a, SV b, SV c, const FaceInfo& F, in
     return true;
 }
 
-// Writes the record of a triangle that passed tri_bbox: vertices, depth plane, id, bbox.
-__device__ __forceinline__ void tri_write(SV a, SV b, SV c, uint32_t id, uint32_t hf, const FaceInfo& F, const int* px,
-                                          TriRec* out) {
+// Depth-plane gradients x256 of a triangle that passed tri_bbox (the float operations
+// of the oracle's plane set-up, in the same order).
+__device__ __forceinline__ void tri_plane(SV a, SV b, SV c, float* ax, float* ay) {
     const long long area2 =
         ((long long)b.X - a.X) * ((long long)c.Y - a.Y) - ((long long)c.X - a.X) * ((long long)b.Y - a.Y);
-    const int* sc = F.sc;
     float fa = (float)area2;
     float e1x = (float)((long long)b.X - a.X), e1y = (float)((long long)b.Y - a.Y);
     float e2x = (float)((long long)c.X - a.X), e2y = (float)((long long)c.Y - a.Y);
     float d1 = b.D - a.D, d2 = c.D - a.D;
     float gx = (d1 * e2y - d2 * e1y) / fa;
     float gy = (d2 * e1x - d1 * e2x) / fa;
-    float ox = (float)((long long)sc[0] * 256 + 128 - a.X), oy = (float)((long long)sc[1] * 256 + 128 - a.Y);
+    *ax = gx * 256.0f;  // exact: a power-of-two scale of a value far from overflow
+    *ay = gy * 256.0f;
+}
+
+// Writes the record of triangles A = (v0,v1,v2) (when okA, box pa) and B = (v0,v2,v3)
+// (when okB, box pb); at least one is set.  The record's box is the union of the two.
+__device__ __forceinline__ void rec_write(const SV* v, bool okA, bool okB, const int* pa, const int* pb, uint32_t id,
+                                          int face, TriRec* out) {
+    float axA = 0.f, ayA = 0.f, axB = 0.f, ayB = 0.f;
+    int bx0, bx1, by0, by1;
+    if (okA) {
+        tri_plane(v[0], v[1], v[2], &axA, &ayA);
+        bx0 = pa[0]; bx1 = pa[1]; by0 = pa[2]; by1 = pa[3];
+        if (okB) {
+            bx0 = min(bx0, pb[0]); bx1 = max(bx1, pb[1]); by0 = min(by0, pb[2]); by1 = max(by1, pb[3]);
+        }
+    } else {
+        bx0 = pb[0]; bx1 = pb[1]; by0 = pb[2]; by1 = pb[3];
+    }
+    if (okB) tri_plane(v[0], v[2], v[3], &axB, &ayB);
+    const uint32_t bx = (uint32_t)bx0 | ((uint32_t)bx1 << 12) | ((uint32_t)face << 24) | (okA ? kRecA : 0u) |
+                        (okB ? kRecB : 0u);
+    const uint32_t by = (uint32_t)by0 | ((uint32_t)by1 << 12);
     int4* o = reinterpret_cast<int4*>(out);
-    o[0] = make_int4(a.X, a.Y, b.X, b.Y);
-    o[1] = make_int4(c.X, c.Y, __float_as_int((a.D + gx * ox) + gy * oy), __float_as_int(gx * 256.0f));
-    o[2] = make_int4(__float_as_int(gy * 256.0f), (int)id, (int)((uint32_t)(uint16_t)px[0] | ((uint32_t)px[1] << 16)),
-                     (int)((uint32_t)(uint16_t)px[2] | ((uint32_t)px[3] << 16)));
-    o[3] = make_int4((int)hf, 0, 0, 0);
+    o[0] = make_int4(v[0].X, v[1].X, v[2].X, v[3].X);
+    o[1] = make_int4(v[0].Y, v[1].Y, v[2].Y, v[3].Y);
+    o[2] = make_int4(__float_as_int(v[0].D), __float_as_int(axA), __float_as_int(axB), __float_as_int(ayA));
+    o[3] = make_int4(__float_as_int(ayB), (int)id, (int)bx, (int)by);
+}
+
+// Union of two clamped boxes (x0, x1, y0, y1) where either may be absent.
+__device__ __forceinline__ void box_union(bool okA, bool okB, const int* pa, const int* pb, int* out) {
+    if (okA && okB) {
+        out[0] = min(pa[0], pb[0]); out[1] = max(pa[1], pb[1]);
+        out[2] = min(pa[2], pb[2]); out[3] = max(pa[3], pb[3]);
+    } else {
+        const int* p = okA ? pa : pb;
+        out[0] = p[0]; out[1] = p[1]; out[2] = p[2]; out[3] = p[3];
+    }
 }
 
 // Adds one to each bin the pixel box px touches; cnt = the hemicube's bin counters
@@ -275,7 +306,10 @@ __device__ __forceinline__ bool snap_vertex(float4 c, float hw, float hh, float 
     return true;
 }
 
-// Fan triangles of a clipped polygon into slots base .. base+pn-3 (culled ones marked dead).
+// Records of a clipped polygon's fan (s0, sj, sj+1), two triangles per record, into slots
+// base .. base + (pn-1)/2 - 1; a record whose triangles are both culled is marked dead.
+__device__ __forceinline__ uint32_t fan_records(int pn) { return pn >= 3 ? (uint32_t)(pn - 1) / 2u : 0u; }
+
 __device__ __noinline__ void emit_polygon(const Geo& g, const Batch& b, const float4* poly, int pn, uint32_t base,
                                           uint32_t p, uint32_t hi, int f, float hw, float hh, float vx, float vy,
                                           uint32_t* cnt, DevState* st) {
@@ -284,15 +318,20 @@ __device__ __noinline__ void emit_polygon(const Geo& g, const Batch& b, const fl
     bool good = true;
     for (int k = 0; k < pn; k++) good = good && snap_vertex(poly[k], hw, hh, vx, vy, sv[k]);
     TriRec* tris = b.tris + (size_t)hi * b.tri_cap_h;  // this hemicube's records
-    for (int j = 0; j + 2 < pn; j++) {
-        const uint32_t slot = base + (uint32_t)j;
+    for (int j = 1, r = 0; j + 1 < pn; j += 2, r++) {
+        const uint32_t slot = base + (uint32_t)r;
         if (slot >= b.tri_cap_h) {
             atomicOr(&st->overflow, 1u);
             return;
         }
-        int px[4];
-        if (good && tri_bbox(sv[0], sv[j + 1], sv[j + 2], F, px)) {
-            tri_write(sv[0], sv[j + 1], sv[j + 2], p, hi * 5 + (uint32_t)f, F, px, &tris[slot]);
+        const bool hasB = j + 2 < pn;
+        SV v[4] = {sv[0], sv[j], sv[j + 1], hasB ? sv[j + 2] : sv[j + 1]};
+        int pa[4], pb[4], px[4];
+        const bool okA = good && tri_bbox(v[0], v[1], v[2], F, pa);
+        const bool okB = good && hasB && tri_bbox(v[0], v[2], v[3], F, pb);
+        if (okA || okB) {
+            rec_write(v, okA, okB, pa, pb, p, f, &tris[slot]);
+            box_union(okA, okB, pa, pb, px);
             count_bins(g, F, px, cnt);
         } else {
             tris[slot].id = kDeadTri;
@@ -421,34 +460,38 @@ __global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* _
         }
         const float hw = 0.5f * (float)F.vp[2], hh = 0.5f * (float)F.vp[3];
         const float vx = (float)F.vp[0], vy = (float)F.vp[1];
-#pragma unroll
-        for (int t = 0; t < 2; t++) {
-            const float4 va = cv[0], vb = cv[1 + t], vc = cv[2 + t];
-            const bool clip = has && (needs_clip(va) || needs_clip(vb) || needs_clip(vc));
-            const bool fast = has && !clip;
-            SV s0, s1, s2;
-            int px[4];
-            bool ok = false;
-            if (fast) {
-                const bool good = snap_vertex(va, hw, hh, vx, vy, s0) & snap_vertex(vb, hw, hh, vx, vy, s1) &
-                                  snap_vertex(vc, hw, hh, vx, vy, s2);
-                ok = good && tri_bbox(s0, s1, s2, F, px);
+        // an item whose four corners need no clipping is one record (both triangles);
+        // otherwise each triangle is clipped and its fan packed two triangles per record
+        const bool clipq =
+            has && (needs_clip(cv[0]) || needs_clip(cv[1]) || needs_clip(cv[2]) || needs_clip(cv[3]));
+        const bool anyclip = __any_sync(0xffffffffu, clipq);
+        for (int t = 0; t < (anyclip ? 2 : 1); t++) {  // warp-uniform trip count
+            SV s[4];
+            int pa[4], pb[4], px[4];
+            bool okA = false, okB = false;
+            if (has && !clipq && t == 0) {
+                const bool g0 = snap_vertex(cv[0], hw, hh, vx, vy, s[0]), g1 = snap_vertex(cv[1], hw, hh, vx, vy, s[1]);
+                const bool g2 = snap_vertex(cv[2], hw, hh, vx, vy, s[2]), g3 = snap_vertex(cv[3], hw, hh, vx, vy, s[3]);
+                okA = g0 && g1 && g2 && tri_bbox(s[0], s[1], s[2], F, pa);
+                okB = g0 && g2 && g3 && tri_bbox(s[0], s[2], s[3], F, pb);
             }
             float4 poly[12];
             int pn = 0;
-            if (clip) {
-                poly[0] = va;
-                poly[1] = vb;
-                poly[2] = vc;
+            if (clipq) {
+                poly[0] = cv[0];
+                poly[1] = cv[1 + t];
+                poly[2] = cv[2 + t];
                 pn = clip_polygon(poly, 3);
             }
-            const uint32_t ncand = fast ? (ok ? 1u : 0u) : (pn >= 3 ? (uint32_t)(pn - 2) : 0u);
+            const bool quad = okA || okB;
+            const uint32_t ncand = quad ? 1u : fan_records(pn);
             // slots are allocated per hemicube (one counter each, not one for the batch)
             const uint32_t base = warp_alloc(&b.tri_counts[hi], ncand);
-            const bool written = fast && ok && base < b.tri_cap_h;
-            if (fast && ok) {
-                if (base >= b.tri_cap_h) atomicOr(&st->overflow, 1u);
-                else tri_write(s0, s1, s2, pp, hi * 5 + (uint32_t)f, F, px, &b.tris[(size_t)hi * b.tri_cap_h + base]);
+            const bool written = quad && base < b.tri_cap_h;
+            if (quad) {
+                if (!written) atomicOr(&st->overflow, 1u);
+                else rec_write(s, okA, okB, pa, pb, pp, f, &b.tris[(size_t)hi * b.tri_cap_h + base]);
+                box_union(okA, okB, pa, pb, px);
             } else if (ncand) {
                 emit_polygon(g, b, poly, pn, base, pp, hi, f, hw, hh, vx, vy, cnt, st);
             }
@@ -518,15 +561,17 @@ __global__ void k_fill(Geo g, Batch b, DevState* st) {
         size_t gb0 = 0;
         uint32_t bins_x = 0;
         if (on) {
-            const TriRec& t = tris[s];
-            on = t.id != kDeadTri;
+            const int4 tail = *reinterpret_cast<const int4*>(&tris[s].ay[1]);  // ay[1], id, bx, by
+            on = (uint32_t)tail.y != kDeadTri;
             if (on) {
-                const uint32_t f = t.hf % 5;
-                const FaceInfo& F = g.face[f];
-                c0 = (t.px0 - F.sc[0]) >> sh;
-                c1 = (t.px1 - F.sc[0]) >> sh;
-                r0 = (t.py0 - F.sc[1]) >> sh;
-                r1 = (t.py1 - F.sc[1]) >> sh;
+                TriRec t;
+                t.bx = (uint32_t)tail.z;
+                t.by = (uint32_t)tail.w;
+                const FaceInfo& F = g.face[rec_face(t)];
+                c0 = (rec_px0(t) - F.sc[0]) >> sh;
+                c1 = (rec_px1(t) - F.sc[0]) >> sh;
+                r0 = (rec_py0(t) - F.sc[1]) >> sh;
+                r1 = (rec_py1(t) - F.sc[1]) >> sh;
                 gb0 = (size_t)hi * g.nb + F.bin_base;
                 bins_x = F.bins_x;
             }
@@ -583,18 +628,30 @@ constexpr int32_t kSmallExtent = 16384;  // 64 px in 24.8 fixed point: edge valu
 constexpr int kChunk = 256;          // triangle records staged per CTA round
 constexpr int kHashSlots = 1024;     // per-bin id -> sum table of the reduction phase
 constexpr uint32_t kHashEmpty = 0xFFFFFFFFu;
-constexpr int kRegionBytes = 12 * kHashSlots;  // >= kChunk * (sizeof(RTri) + 8) (12 KB)
 constexpr int kSizeClasses = 16;               // ceil(log2(box pixels)) for boxes <= 2^15 px
-constexpr int kMaxPieces = 8;                  // pieces per small triangle (g.piece >= small_max / 8)
+constexpr int kMaxPieces = 8;                  // pieces per small record (g.piece >= small_max / 8)
 
-// The parts of a triangle record the per-pixel loops need (40 bytes in shared memory).
+// The parts of a record the per-pixel loops need (68 bytes in shared memory): the
+// two triangles A = (v0,v1,v2), B = (v0,v2,v3) with their depth planes.
+struct RQuad {
+    int32_t X[4], Y[4];
+    float c0[2], ax[2], ay[2];
+    uint32_t id, flags;  // flags: kRecA | kRecB
+    uint32_t pad;        // 17-word stride: lanes reading different records hit different banks
+};
+// One triangle, for the warp path.
 struct RTri {
     int32_t X[3], Y[3];
     float c0, ax, ay;
     uint32_t id;
 };
-static_assert(kChunk * (sizeof(RTri) + sizeof(short4)) <= (size_t)kRegionBytes, "chunk staging exceeds the region");
+// one region, two uses: the chunk's records + clamped boxes, then the reduction's hash table
+constexpr int kStageBytes = kChunk * (int)(sizeof(RQuad) + sizeof(short4));
+constexpr int kRegionBytes = kStageBytes > 12 * kHashSlots ? kStageBytes : 12 * kHashSlots;  // 19 KB
+static_assert(kChunk * sizeof(RQuad) % 8 == 0, "clamped boxes follow the records");
 static_assert(kChunk <= 256, "chunk indices are stored as uint8");
+template <int TILE>
+constexpr int raster_dyn_smem() { return TILE * TILE * 8 + kRegionBytes; }
 
 __device__ __forceinline__ bool inside_edge(long long e, bool tl) { return e > 0 || (e == 0 && tl); }
 __device__ __forceinline__ bool inside_edge32(int32_t e, bool tl) { return e > 0 || (e == 0 && tl); }
@@ -644,49 +701,75 @@ __device__ __forceinline__ void hash_add(uint32_t* h_id, unsigned long long* h_s
     atomicAdd(&Fq[id], sum);
 }
 
-// One lane rasterises pixels [start, start + steps) of a small triangle's clamped bbox
+// One lane rasterises pixels [start, start + steps) of a small record's clamped bbox
 // [x0,x1]x[y0,y1] (row-major flat order) with 32-bit incremental edge functions (exact:
-// |E| < 2^30 for extents <= 64 px), one flat loop of `steps` iterations.
+// |E| < 2^30 for extents <= 64 px), one flat loop of `steps` iterations.  Six edges:
+// A = v0->v1, v1->v2, v2->v0 and B = v0->v2, v2->v3, v3->v0, each with its own
+// top-left flag.  Each is tracked as f = E + tl - 1, so "inside" (E > 0, or E == 0 on
+// a top-left edge) is f >= 0 and a triangle covers the pixel iff the OR of its three
+// f is >= 0; a triangle absent from the record has one f pinned at -1.  A pixel inside
+// both (possible only where a record's snapped outline folds over) takes the smaller
+// key, as two separate draws would.  The record's fields are copied to registers
+// first: the atomics write shared memory, so reads through `t` would be repeated.
 template <int TILE>
-__device__ __forceinline__ void raster_small(const RTri& t, int x0, int x1, int y0, int start, int steps,
+__device__ __forceinline__ void raster_small(const RQuad& t, int x0, int x1, int y0, int start, int steps,
                                              const BinInfo& bi, int sx, int sy, unsigned long long* key) {
     const int w = x1 - x0 + 1;
     const int ry = start / w, rx = start - ry * w;
     int px = x0 + rx, py = y0 + ry;
-    int32_t er[3], e[3], stx[3], sty[3];
-    bool tl[3];
+    const float c0a = t.c0[0], axa = t.ax[0], aya = t.ay[0];
+    const float c0b = t.c0[1], axb = t.ax[1], ayb = t.ay[1];
+    const uint32_t id = t.id, flags = t.flags;
+    int32_t f[6], st[6], rs[6];
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-        const int j = k == 2 ? 0 : k + 1;
-        const int32_t dx = t.X[j] - t.X[k], dy = t.Y[j] - t.Y[k];
-        er[k] = dx * (py * 256 + 128 - t.Y[k]) - dy * (x0 * 256 + 128 - t.X[k]);
-        stx[k] = -dy * 256;
-        sty[k] = dx * 256;
-        e[k] = er[k] + stx[k] * rx;
-        tl[k] = (t.Y[j] < t.Y[k]) || (t.Y[j] == t.Y[k] && t.X[j] < t.X[k]);
+    for (int k = 0; k < 6; k++) {
+        const int a = k == 0 ? 0 : (k == 1 ? 1 : (k == 2 ? 2 : (k == 3 ? 0 : (k == 4 ? 2 : 3))));  // from
+        const int j = k == 0 ? 1 : (k == 1 ? 2 : (k == 2 ? 0 : (k == 3 ? 2 : (k == 4 ? 3 : 0))));  // to
+        const int32_t dx = t.X[j] - t.X[a], dy = t.Y[j] - t.Y[a];
+        const bool tl = (t.Y[j] < t.Y[a]) || (t.Y[j] == t.Y[a] && t.X[j] < t.X[a]);
+        f[k] = dx * (py * 256 + 128 - t.Y[a]) - dy * (px * 256 + 128 - t.X[a]) - (tl ? 0 : 1);
+        st[k] = -dy * 256;                  // one pixel right
+        rs[k] = dx * 256 + dy * 256 * (w - 1);  // from (x1, y) to (x0, y + 1)
     }
-    int row = (py - bi.y0) * TILE - (int)bi.x0;  // key index of pixel (px, py) = row + px
+    if (!(flags & kRecA)) f[0] = -1, st[0] = 0, rs[0] = 0;
+    if (!(flags & kRecB)) f[3] = -1, st[3] = 0, rs[3] = 0;
+    int idx = (py - bi.y0) * TILE + (px - bi.x0);
+    const int rowjump = TILE - (w - 1);
     for (int i = 0; i < steps; i++) {
-        if (inside_edge32(e[0], tl[0]) && inside_edge32(e[1], tl[1]) && inside_edge32(e[2], tl[2])) {
+        const int32_t ca = f[0] | f[1] | f[2], cb = f[3] | f[4] | f[5];
+        if ((ca & cb) >= 0) {
             const float u = (float)(px - sx), wv = (float)(py - sy);
-            const float D = (t.c0 + t.ax * u) + t.ay * wv;
-            atomicMin(&key[row + px], ((unsigned long long)depth_ordinal(D) << 32) | t.id);
-        }
-        if (px < x1) {
-            px++;
-#pragma unroll
-            for (int k = 0; k < 3; k++) e[k] += stx[k];
-        } else {
-            px = x0;
-            py++;
-            row += TILE;
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                er[k] += sty[k];
-                e[k] = er[k];
+            unsigned long long k = ~0ull;
+            if (ca >= 0) k = ((unsigned long long)depth_ordinal((c0a + axa * u) + aya * wv) << 32) | id;
+            if (cb >= 0) {
+                const unsigned long long kb = ((unsigned long long)depth_ordinal((c0b + axb * u) + ayb * wv) << 32) | id;
+                k = kb < k ? kb : k;
             }
+            atomicMin(&key[idx], k);
         }
+        const bool wrap = px == x1;
+        px = wrap ? x0 : px + 1;
+        py += wrap ? 1 : 0;
+        idx += wrap ? rowjump : 1;
+#pragma unroll
+        for (int k = 0; k < 6; k++) f[k] += wrap ? rs[k] : st[k];
     }
+}
+
+// Triangle A (which = 0) or B (which = 1) of a record, for the warp path.
+__device__ __forceinline__ RTri rec_tri(const RQuad& q, int which) {
+    RTri t;
+    t.X[0] = q.X[0];
+    t.Y[0] = q.Y[0];
+    t.X[1] = q.X[1 + which];
+    t.Y[1] = q.Y[1 + which];
+    t.X[2] = q.X[2 + which];
+    t.Y[2] = q.Y[2 + which];
+    t.c0 = q.c0[which];
+    t.ax = q.ax[which];
+    t.ay = q.ay[which];
+    t.id = q.id;
+    return t;
 }
 
 // One warp rasterises a large triangle in 8x4 stamps.  The 32 lanes first
@@ -788,12 +871,14 @@ __global__ void __launch_bounds__(256, 4) k_raster(Geo g, Batch b, const float* 
     const uint32_t hi = gb / g.nb, bin = gb % g.nb;
     const BinInfo bi = b.bins[bin];
     const bool valid = b.valid[hi] != 0;
-    __shared__ unsigned long long key[TILE * TILE];
-    // one region, two uses: the chunk's triangles (records + clamped boxes) during the
-    // raster phase, then the per-bin id -> exact-sum hash table of the reduction phase
-    __shared__ __align__(16) unsigned char s_region[kRegionBytes];
-    RTri* s_tri = reinterpret_cast<RTri*>(s_region);
-    short4* s_box = reinterpret_cast<short4*>(s_region + kChunk * sizeof(RTri));
+    // dynamic shared memory: the bin's depth|id keys, then one region with two uses: the
+    // chunk's records + clamped boxes during the raster phase, then the per-bin
+    // id -> exact-sum hash table of the reduction phase
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    unsigned long long* key = reinterpret_cast<unsigned long long*>(s_dyn);
+    unsigned char* s_region = s_dyn + TILE * TILE * 8;
+    RQuad* s_tri = reinterpret_cast<RQuad*>(s_region);
+    short4* s_box = reinterpret_cast<short4*>(s_region + kChunk * sizeof(RQuad));
     __shared__ uint8_t s_order[kChunk];  // small triangles by size class (ascending)
     __shared__ uint8_t s_bigi[kChunk];   // big triangles
     __shared__ uint32_t s_ncls[kSizeClasses];
@@ -824,22 +909,34 @@ __global__ void __launch_bounds__(256, 4) k_raster(Geo g, Batch b, const float* 
             int cls = -1;
             uint32_t rank = 0;
             if (threadIdx.x < m) {
-                const TriRec& tr = b.tris[b.bin_list[off + base + threadIdx.x]];
-                const int4 a = *reinterpret_cast<const int4*>(&tr.X0);
-                const int4 c = *reinterpret_cast<const int4*>(&tr.X2);
-                const int4 d = *reinterpret_cast<const int4*>(&tr.ay);
-                RTri t;
-                t.X[0] = a.x; t.Y[0] = a.y; t.X[1] = a.z; t.Y[1] = a.w;
-                t.X[2] = c.x; t.Y[2] = c.y; t.c0 = __int_as_float(c.z); t.ax = __int_as_float(c.w);
-                t.ay = __int_as_float(d.x); t.id = (uint32_t)d.y;
-                const int px0 = (int)(int16_t)(d.z & 0xFFFF), px1 = (int)(int16_t)((uint32_t)d.z >> 16);
-                const int py0 = (int)(int16_t)(d.w & 0xFFFF), py1 = (int)(int16_t)((uint32_t)d.w >> 16);
+                const int4* tr = reinterpret_cast<const int4*>(&b.tris[b.bin_list[off + base + threadIdx.x]]);
+                const int4 xs = tr[0], ys = tr[1], p = tr[2], q = tr[3];  // q = ay[1], id, bx, by
+                const int px0 = q.z & 0xFFF, px1 = (q.z >> 12) & 0xFFF;
+                const int py0 = q.w & 0xFFF, py1 = (q.w >> 12) & 0xFFF;
                 const int x0 = max(px0, (int)bi.x0), x1 = min(px1, bx1);
                 const int y0 = max(py0, (int)bi.y0), y1 = min(py1, by1);
                 if (x0 <= x1 && y0 <= y1) {
+                    RQuad t;
+                    t.X[0] = xs.x; t.X[1] = xs.y; t.X[2] = xs.z; t.X[3] = xs.w;
+                    t.Y[0] = ys.x; t.Y[1] = ys.y; t.Y[2] = ys.z; t.Y[3] = ys.w;
+                    // the planes' constant terms at the scissor origin, rebuilt with the
+                    // set-up's float operations (gx = ax / 256 exactly)
+                    const float d0 = __int_as_float(p.x);
+                    const float ox = (float)((long long)sx * 256 + 128 - xs.x);
+                    const float oy = (float)((long long)sy * 256 + 128 - ys.x);
+                    t.ax[0] = __int_as_float(p.y);
+                    t.ax[1] = __int_as_float(p.z);
+                    t.ay[0] = __int_as_float(p.w);
+                    t.ay[1] = __int_as_float(q.x);
+                    t.c0[0] = (d0 + (t.ax[0] * 0x1p-8f) * ox) + (t.ay[0] * 0x1p-8f) * oy;
+                    t.c0[1] = (d0 + (t.ax[1] * 0x1p-8f) * ox) + (t.ay[1] * 0x1p-8f) * oy;
+                    t.id = (uint32_t)q.y;
+                    t.flags = (uint32_t)q.z & (kRecA | kRecB);
                     s_tri[threadIdx.x] = t;
-                    const int32_t ex = max(t.X[0], max(t.X[1], t.X[2])) - min(t.X[0], min(t.X[1], t.X[2]));
-                    const int32_t ey = max(t.Y[0], max(t.Y[1], t.Y[2])) - min(t.Y[0], min(t.Y[1], t.Y[2]));
+                    const int32_t ex = max(max(t.X[0], t.X[1]), max(t.X[2], t.X[3])) -
+                                       min(min(t.X[0], t.X[1]), min(t.X[2], t.X[3]));
+                    const int32_t ey = max(max(t.Y[0], t.Y[1]), max(t.Y[2], t.Y[3])) -
+                                       min(min(t.Y[0], t.Y[1]), min(t.Y[2], t.Y[3]));
                     const int area = (x1 - x0 + 1) * (y1 - y0 + 1);
                     if (ex <= kSmallExtent && ey <= kSmallExtent && area <= (int)g.small_max) {
                         s_box[threadIdx.x] = make_short4((short)x0, (short)x1, (short)y0, (short)y1);
@@ -894,8 +991,12 @@ __global__ void __launch_bounds__(256, 4) k_raster(Geo g, Batch b, const float* 
                 const int start = (gp - (int)s_poff[pos]) * per;
                 raster_small<TILE>(s_tri[i], bx.x, bx.y, bx.z, start, min(per, area - start), bi, sx, sy, key);
             }
-            for (int i = (int)(threadIdx.x >> 5); i < nbig; i += (int)(blockDim.x >> 5)) {
-                const RTri t = s_tri[s_bigi[i]];
+            // big records: one warp per triangle of the record (A, then B)
+            for (int i = (int)(threadIdx.x >> 5); i < 2 * nbig; i += (int)(blockDim.x >> 5)) {
+                const RQuad& q = s_tri[s_bigi[i >> 1]];
+                const int which = i & 1;
+                if (!(q.flags & (which ? kRecB : kRecA))) continue;
+                const RTri t = rec_tri(q, which);
                 const int32_t xmn = min(t.X[0], min(t.X[1], t.X[2])), xmx = max(t.X[0], max(t.X[1], t.X[2]));
                 const int32_t ymn = min(t.Y[0], min(t.Y[1], t.Y[2])), ymx = max(t.Y[0], max(t.Y[1], t.Y[2]));
                 const int x0 = max((int)floordiv256((long long)xmn - 128 + 255), (int)bi.x0);
@@ -964,13 +1065,36 @@ __global__ void __launch_bounds__(256, 4) k_raster(Geo g, Batch b, const float* 
     }
 }
 
+template <int TILE>
+static cudaError_t raster_attrs() {
+    cudaError_t e = cudaFuncSetAttribute(k_raster<TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         raster_dyn_smem<TILE>());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_raster<TILE>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
+    return e;
+}
+
+cudaError_t raster_init() {
+    cudaError_t e = raster_attrs<16>();
+    if (e == cudaSuccess) e = raster_attrs<32>();
+    if (e == cudaSuccess) e = raster_attrs<64>();
+    return e;
+}
+
 void launch_raster(const Geo& g, const Batch& b, const float* fftab, DevState* st, bool write_items,
                    bool fused_reduce, cudaStream_t s, bool count) {
     dim3 grid(b.K * g.nb);
     switch (g.tile) {
-        case 16: k_raster<16><<<grid, 256, 0, s>>>(g, b, fftab, st, write_items, fused_reduce, count); break;
-        case 64: k_raster<64><<<grid, 256, 0, s>>>(g, b, fftab, st, write_items, fused_reduce, count); break;
-        default: k_raster<32><<<grid, 256, 0, s>>>(g, b, fftab, st, write_items, fused_reduce, count); break;
+        case 16:
+            k_raster<16><<<grid, 256, raster_dyn_smem<16>(), s>>>(g, b, fftab, st, write_items, fused_reduce, count);
+            break;
+        case 64:
+            k_raster<64><<<grid, 256, raster_dyn_smem<64>(), s>>>(g, b, fftab, st, write_items, fused_reduce, count);
+            break;
+        default:
+            k_raster<32><<<grid, 256, raster_dyn_smem<32>(), s>>>(g, b, fftab, st, write_items, fused_reduce, count);
+            break;
     }
 }
 
