@@ -29,10 +29,13 @@ namespace rad {
 // ---------------------------------------------------------------------------
 // Row capture: exact sums -> FP32 rows, BF16 rows + per-row scale
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_dense_rows(const unsigned long long* __restrict__ Fq, uint32_t n, uint32_t ld,
+// One CTA per captured row: exact sums -> FP32 row (optional), BF16 row scaled by the
+// row maximum, and the scale.  The sums are zeroed after their last read, ready for the
+// next chunk of rows.
+__global__ void __launch_bounds__(256) k_dense_rows(unsigned long long* __restrict__ Fq, uint32_t n, uint32_t ld,
                                                     uint32_t first, float* F32, __nv_bfloat16* F16, float* scale) {
     const uint32_t r = blockIdx.x;  // row within the batch
-    const unsigned long long* src = Fq + (size_t)r * n;
+    unsigned long long* src = Fq + (size_t)r * n;
     const size_t row = (size_t)(first + r);
     __shared__ float red[256];
     float mx = 0.f;
@@ -50,13 +53,17 @@ __global__ void __launch_bounds__(256) k_dense_rows(const unsigned long long* __
     const float s = red[0] > 0.f ? red[0] : 1.0f;
     const float inv = 1.0f / s;
     for (uint32_t j = threadIdx.x; j < ld; j += blockDim.x) {
-        const float f = j < n ? __ull2float_rn(src[j]) * 0x1p-61f : 0.f;
+        float f = 0.f;
+        if (j < n) {
+            f = __ull2float_rn(src[j]) * 0x1p-61f;
+            src[j] = 0ull;
+        }
         F16[row * ld + j] = __float2bfloat16_rn(f * inv);
     }
     if (threadIdx.x == 0) scale[row] = s;
 }
 
-void launch_dense_rows(const unsigned long long* Fq, uint32_t count, uint32_t n, uint32_t ld, uint32_t first,
+void launch_dense_rows(unsigned long long* Fq, uint32_t count, uint32_t n, uint32_t ld, uint32_t first,
                        float* F32, __nv_bfloat16* F16, float* scale, cudaStream_t s) {
     k_dense_rows<<<count, 256, 0, s>>>(Fq, n, ld, first, F32, F16, scale);
 }

@@ -768,6 +768,10 @@ int rad_autotune(rad_ctx* c, uint32_t flags, rad_tuning* out) {
     return RAD_OK;
 }
 
+// Every form-factor row, 128 shooters per chunk, queued back to back on the context's
+// stream: the chunk's shooter ids are a slice of one device array of 0..n-1, the row
+// conversion zeroes the exact sums it has read (so the next chunk starts from zero), and
+// the capacity flags are read once at the end.
 int rad_dense_capture(rad_ctx* c, uint32_t flags, double* device_ms) {
     if (!c) return RAD_E_INVALID;
     if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
@@ -780,29 +784,53 @@ int rad_dense_capture(rad_ctx* c, uint32_t flags, double* device_ms) {
     RAD_CUDA(c, cudaMalloc(&c->d_F16, sizeof(__nv_bfloat16) * (size_t)n * ld));
     RAD_CUDA(c, cudaMalloc(&c->d_scale, sizeof(float) * n));
     if (flags & RAD_DENSE_FP32) RAD_CUDA(c, cudaMalloc(&c->d_F32, sizeof(float) * (size_t)n * ld));
-    const uint32_t chunk = 128;
-    std::vector<uint32_t> ids(chunk);
-    cudaEvent_t e0, e1;
-    RAD_CUDA(c, cudaEventCreate(&e0));
-    RAD_CUDA(c, cudaEventCreate(&e1));
-    RAD_CUDA(c, cudaEventRecord(e0, c->stream));
-    for (uint32_t first = 0; first < n; first += chunk) {
+    const uint32_t chunk = std::min<uint32_t>(128, n);
+    int rc = alloc_batch(c, c->aux, chunk, false);
+    if (rc) return rc;
+    cudaStream_t s = c->stream;
+    uint32_t* d_ids = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto done = [&](int code) {
+        if (d_ids) cudaFree(d_ids);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        return code;
+    };
+    std::vector<uint32_t> ids(n), ones(chunk, 1u);
+    for (uint32_t i = 0; i < n; i++) ids[i] = i;
+    if (cudaMalloc(&d_ids, sizeof(uint32_t) * n) != cudaSuccess) return done(fail(c, RAD_E_NOMEM, "cudaMalloc ids"));
+    Batch b = c->aux.b;
+    bool ok = cudaMemcpyAsync(d_ids, ids.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+              cudaMemcpyAsync(b.valid, ones.data(), sizeof(uint32_t) * chunk, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+              cudaMemsetAsync(c->d_aux, 0, sizeof(DevState), s) == cudaSuccess &&
+              cudaMemsetAsync(b.Fq, 0, sizeof(unsigned long long) * (size_t)chunk * n, s) == cudaSuccess &&
+              cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess &&
+              cudaEventRecord(e0, s) == cudaSuccess;
+    for (uint32_t first = 0; ok && first < n; first += chunk) {
         const uint32_t cnt = std::min(chunk, n - first);
-        for (uint32_t k = 0; k < cnt; k++) ids[k] = first + k;
-        int rc = run_aux(c, ids.data(), cnt, false, true);
-        if (rc) return rc;
-        launch_dense_rows(c->aux.b.Fq, cnt, n, ld, first, c->d_F32, c->d_F16, c->d_scale, c->stream);
-        RAD_CUDA(c, cudaGetLastError());
+        b.K = cnt;
+        b.shooters = d_ids + first;
+        ok = cudaMemsetAsync(b.tri_counts, 0, sizeof(uint32_t) * cnt, s) == cudaSuccess &&
+             cudaMemsetAsync(b.bin_count, 0, sizeof(uint32_t) * (size_t)cnt * c->geo.nb, s) == cudaSuccess;
+        if (!ok) break;
+        launch_camera(c->geo, b, c->d_verts, c->d_rad, c->d_aux, s);
+        launch_setup(c->geo, b, c->d_verts, c->d_aux, s);
+        launch_bins(c->geo, b, c->d_aux, s);
+        launch_raster(c->geo, b, c->d_fftab, c->d_aux, false, true, s);
+        launch_dense_rows(b.Fq, cnt, n, ld, first, c->d_F32, c->d_F16, c->d_scale, s);
+        ok = cudaGetLastError() == cudaSuccess;
     }
-    RAD_CUDA(c, cudaEventRecord(e1, c->stream));
-    RAD_CUDA(c, cudaEventSynchronize(e1));
+    ok = ok && cudaEventRecord(e1, s) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess;
+    if (!ok) return done(fail(c, RAD_E_CUDA, "dense capture: CUDA error"));
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    DevState st;
+    if (cudaMemcpy(&st, c->d_aux, sizeof(st), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return done(fail(c, RAD_E_CUDA, "dense capture: state read"));
+    if (st.overflow) return done(fail(c, RAD_E_OVERFLOW, "triangle or bin capacity exceeded"));
     if (device_ms) *device_ms = ms;
     c->dense_ready = true;
-    return RAD_OK;
+    return done(RAD_OK);
 }
 
 int rad_dense_rows(rad_ctx* c, uint32_t first, uint32_t count, float* f32, uint16_t* bf16, float* scale) {

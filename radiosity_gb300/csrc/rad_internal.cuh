@@ -149,7 +149,7 @@ struct TcEpilogue {
     uint32_t ld16;
     uint32_t* err;
 };
-void launch_dense_rows(const unsigned long long* Fq, uint32_t count, uint32_t n, uint32_t ld, uint32_t first,
+void launch_dense_rows(unsigned long long* Fq, uint32_t count, uint32_t n, uint32_t ld, uint32_t first,
                        float* F32, __nv_bfloat16* F16, float* scale, cudaStream_t s);
 void launch_sgemm_resid(const float* F, uint32_t n, uint32_t ld, const float* X, const float* E, const float4* rho,
                         uint32_t R, float* r, double* nrm, cudaStream_t s);
