@@ -236,6 +236,65 @@ int rad_raster_counters(rad_ctx* ctx, uint64_t* out);
 int rad_scene_reference(double max_patch_area, uint32_t capacity, uint32_t* n, float* vertices,
                         int32_t* indices, float* color, float* radiosity, float* illumination);
 
+/* ---- Scene inputs, display output and checkpoints around the shoot loop --------------- */
+
+/* The 8 display neighbours of every patch of the reference scene (N x 8 scene indices,
+ * numbered from the upper left corner clockwise; a patch that was not divided is its own
+ * neighbour): Patch::neighbours as set by Patch::divide (source/Patch.cpp:128-219) and
+ * Model::subdivide (source/Model.cpp:38-46).  Same calling convention as rad_scene_reference. */
+int rad_scene_reference_neighbours(double max_patch_area, uint32_t capacity, uint32_t* n, uint32_t* neighbours);
+
+/* WaveFrontModel (source/WaveFrontModel.cpp:15-143) on an in-memory OBJ file of `length`
+ * bytes, subdivided to max_patch_area (0 = not subdivided) as ModelContainer does: "v"
+ * lines scaled by 1/1000, "f" lines with 3 or 4 vertices (a triangle repeats its last
+ * vertex), other faces and faces naming a missing vertex skipped.  Patches are black with
+ * no energy.  RAD_E_INVALID on a vertex line with fewer than 3 coordinates (the
+ * reference's parse error).  Outputs as rad_scene_reference plus the neighbours (N x 8);
+ * any array may be NULL; call with all NULL to get *n. */
+int rad_scene_obj(const char* text, uint64_t length, double max_patch_area, uint32_t capacity, uint32_t* n,
+                  float* vertices, int32_t* indices, float* color, float* radiosity, float* illumination,
+                  uint32_t* neighbours);
+
+/* .rr scene files of SaveToFile / LoadFromFile (source/Main.cpp:1460-1647,
+ * source/LoadingModel.cpp:4-17): a 32-bit patch count, then the reference's Patch
+ * objects as raw bytes (radiosity, illumination, relativeNeighbours[8], neighbours[8]
+ * written as NULL pointers, the 4 corners, color), 148 bytes each from a 32-bit build
+ * (pointer_bytes = 4) or 184 bytes from a 64-bit build (pointer_bytes = 8).  rad_rr_write
+ * writes such a file into out (rad_rr_size bytes; neighbours may be NULL = each patch its
+ * own); rad_rr_read detects the build from the file size and returns the scene (patches in
+ * file order, not subdivided again, as LoadingModel) with *pointer_bytes; RAD_E_INVALID on
+ * a size that fits neither build or a neighbour index out of range. */
+int rad_rr_size(uint32_t n, uint32_t pointer_bytes, uint64_t* bytes);
+int rad_rr_write(uint32_t n, const float* vertices, const float* color, const float* radiosity,
+                 const float* illumination, const uint32_t* neighbours, uint32_t pointer_bytes, void* out,
+                 uint64_t capacity);
+int rad_rr_read(const void* data, uint64_t length, uint32_t capacity, uint32_t* n, float* vertices, int32_t* indices,
+                float* color, float* radiosity, float* illumination, uint32_t* neighbours, uint32_t* pointer_bytes);
+
+/* Uploads the scene's display neighbours (N x 8 patch indices, e.g. from
+ * rad_scene_reference_neighbours / rad_scene_obj / rad_rr_read) for rad_display_colors. */
+int rad_upload_neighbours(rad_ctx* ctx, const uint32_t* neighbours);
+
+/* The display update after a batch of shots (source/Main.cpp:1318-1372) on the
+ * device-resident state: colors = Colors::smoothShadePatch of every patch
+ * (source/Colors.cpp:198-262; needs rad_upload_neighbours), radiative = each patch's
+ * radiosity at its 4 corners; N x 12 floats each in the reference's VBO layout, either
+ * may be NULL.  rad_display_colors copies them to host arrays; rad_display_colors_device
+ * writes caller-owned device buffers (a headless stand-in for the mapped GL VBOs). */
+int rad_display_colors(rad_ctx* ctx, float* colors, float* radiative);
+int rad_display_colors_device(rad_ctx* ctx, float* d_colors, float* d_radiative);
+
+/* ModelContainer::getHighestRadiosityPatchId (source/ModelContainer.cpp:222-237) on the
+ * device-resident state: the first patch with the largest |radiosity|^2; PHYS mode: the
+ * first with the largest unshot power (r+g+b)*area. */
+int rad_highest_patch(rad_ctx* ctx, uint32_t* id);
+
+/* Progress of the shoot loop for checkpoint / resume: batches done so far and the initial
+ * unshot power that the PHYS residual is relative to (set by rad_upload_scene).  Restore
+ * both after re-uploading a saved state so that the residual and stop rule continue. */
+int rad_progress(rad_ctx* ctx, uint32_t* shots_done, double* initial_power);
+int rad_set_progress(rad_ctx* ctx, uint32_t shots_done, double initial_power);
+
 /* Allocation-free form-factor rows.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory (their device memory belongs to another
  * allocator's pool, or their loop must not allocate per call).  Inputs and outputs are

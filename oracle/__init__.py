@@ -193,9 +193,22 @@ class RefLib:
         L.ref_topk.argtypes = [ctypes.c_uint, _f32p, _u32p, _i32p]
         L.ref_face_mvp.argtypes = [_f32p, ctypes.c_int, _f32p]
         L.ref_patch_frame.argtypes = [_f32p, _f32p]
+        vp = ctypes.c_void_p
+        L.ref_neighbours.argtypes = [_u32p]
+        L.ref_smooth_shade.argtypes = [_f32p, _f32p, _f32p]
+        L.ref_highest_id.argtypes = [_f32p]
+        L.ref_highest_id.restype = ctypes.c_uint
+        L.ref_obj_build.argtypes = [ctypes.c_char_p, ctypes.c_double]
+        L.ref_obj_build.restype = ctypes.c_uint
+        L.ref_obj_get.argtypes = [vp, vp, vp, vp, vp]
+        L.ref_rr_save.argtypes = [_f32p, _f32p, vp, ctypes.POINTER(ctypes.c_uint)]
+        L.ref_rr_save.restype = ctypes.c_ulonglong
+        L.ref_rr_load.argtypes = [vp]
+        L.ref_rr_load.restype = ctypes.c_uint
 
     def scene(self, area: float):
         n = self.L.ref_scene_build(area)
+        self._n = n
         v = np.zeros(12 * n, np.float32)
         idx = np.zeros(6 * n, np.int32)
         col = np.zeros(3 * n, np.float32)
@@ -230,6 +243,48 @@ class RefLib:
         out = np.zeros(9, np.float32)
         self.L.ref_patch_frame(np.ascontiguousarray(quad, np.float32), out)
         return out
+
+    def neighbours(self) -> np.ndarray:
+        """Display neighbours of the last scene(area), N x 8 scene indices."""
+        out = np.zeros(8 * self._n, np.uint32)
+        self.L.ref_neighbours(out)
+        return out
+
+    def smooth_shade(self, rad: np.ndarray, illum: np.ndarray) -> np.ndarray:
+        """Colors::smoothShadePatch of every patch of the last scene(area), N x 12."""
+        out = np.zeros(12 * self._n, np.float32)
+        self.L.ref_smooth_shade(np.ascontiguousarray(rad, np.float32), np.ascontiguousarray(illum, np.float32), out)
+        return out
+
+    def highest_id(self, rad: np.ndarray) -> int:
+        return int(self.L.ref_highest_id(np.ascontiguousarray(rad, np.float32)))
+
+    def _container(self, n: int) -> dict:
+        out = dict(n=n, vertices=np.zeros(12 * n, np.float32), color=np.zeros(3 * n, np.float32),
+                   radiosity=np.zeros(3 * n, np.float32), illumination=np.zeros(3 * n, np.float32),
+                   neighbours=np.zeros(8 * n, np.uint32))
+        self.L.ref_obj_get(*[out[k].ctypes.data_as(ctypes.c_void_p)
+                             for k in ("vertices", "color", "radiosity", "illumination", "neighbours")])
+        return out
+
+    def obj(self, path: str, area: float) -> dict:
+        """WaveFrontModel(path) in a ModelContainer subdivided to `area`."""
+        return self._container(self.L.ref_obj_build(path.encode(), area))
+
+    def rr_save(self, rad: np.ndarray, illum: np.ndarray):
+        """SaveToFile's bytes for the last scene(area) with the given state, and sizeof(Patch)."""
+        rec = ctypes.c_uint(0)
+        r = np.ascontiguousarray(rad, np.float32)
+        i = np.ascontiguousarray(illum, np.float32)
+        size = self.L.ref_rr_save(r, i, None, ctypes.byref(rec))
+        buf = np.zeros(size, np.uint8)
+        self.L.ref_rr_save(r, i, buf.ctypes.data_as(ctypes.c_void_p), ctypes.byref(rec))
+        return buf.tobytes(), rec.value
+
+    def rr_load(self, data: bytes) -> dict:
+        """LoadFromFile + LoadingModel on this build's layout."""
+        raw = np.frombuffer(data, np.uint8).copy()
+        return self._container(self.L.ref_rr_load(raw.ctypes.data_as(ctypes.c_void_p)))
 
     @staticmethod
     def ff_sum_printed(W: int) -> float:

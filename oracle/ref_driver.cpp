@@ -9,6 +9,12 @@
 //   ref_topk         ModelContainer::getHighestRadiosityPatchesId (source/ModelContainer.cpp:313-353)
 //   ref_face_mvp     the per-face MVP of the shoot loop      (source/Main.cpp:1166-1184)
 //   ref_config_*     Config::freeze and its getters          (source/Config.cpp:30-48)
+//   ref_neighbours   Patch::neighbours as scene indices      (source/Patch.cpp:128-219)
+//   ref_smooth_shade Colors::smoothShadePatch per patch      (source/Colors.cpp:198-262)
+//   ref_highest_id   ModelContainer::getHighestRadiosityPatchId (source/ModelContainer.cpp:222-237)
+//   ref_obj_*        WaveFrontModel + ModelContainer         (source/WaveFrontModel.cpp:15-143)
+//   ref_rr_save      SaveToFile's Patch array and byte dump  (source/Main.cpp:1592-1625)
+//   ref_rr_load      LoadFromFile + LoadingModel             (source/Main.cpp:1492-1517, source/LoadingModel.cpp:4-17)
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -26,12 +32,46 @@
 #include "FormFactors.h"
 #include "ModelContainer.h"
 #include "Camera.h"
+#include "Colors.h"
+#include "LoadingModel.h"
 #include "Transform.h"
+#include "WaveFrontModel.h"
 #undef private
 #undef protected
 #include <cstring>
 
 static ModelContainer* g_scene = 0;
+static ModelContainer* g_obj = 0;
+
+// Scene index of every neighbour pointer of container m's patches (N x 8).
+static void neighbours_of(ModelContainer* m, unsigned* nb) {
+    unsigned n = m->getPatchesCount();
+    Patch** p = m->getPatches();
+    std::vector<std::pair<Patch*, unsigned> > idx(n);
+    for (unsigned i = 0; i < n; i++) idx[i] = std::make_pair(p[i], i);
+    std::sort(idx.begin(), idx.end());
+    for (unsigned i = 0; i < n; i++)
+        for (unsigned j = 0; j < 8; j++) {
+            std::pair<Patch*, unsigned> key(p[i]->neighbours[j], 0);
+            std::vector<std::pair<Patch*, unsigned> >::iterator it = std::lower_bound(idx.begin(), idx.end(), key);
+            nb[8 * i + j] = (it != idx.end() && it->first == key.first) ? it->second : 0xFFFFFFFFu;
+        }
+}
+
+static void export_of(ModelContainer* m, float* vertices, float* color, float* rad, float* illum) {
+    unsigned n = m->getPatchesCount();
+    if (vertices) std::memcpy(vertices, m->getVertices(), sizeof(float) * m->getVerticesCount());
+    Patch** p = m->getPatches();
+    for (unsigned i = 0; i < n; i++) {
+        Vector3f c = p[i]->getColor();
+        if (color) { color[3 * i] = c.x; color[3 * i + 1] = c.y; color[3 * i + 2] = c.z; }
+        if (rad) { rad[3 * i] = p[i]->radiosity.x; rad[3 * i + 1] = p[i]->radiosity.y; rad[3 * i + 2] = p[i]->radiosity.z; }
+        if (illum) {
+            illum[3 * i] = p[i]->illumination.x; illum[3 * i + 1] = p[i]->illumination.y;
+            illum[3 * i + 2] = p[i]->illumination.z;
+        }
+    }
+}
 
 static void config_set(unsigned W, unsigned K, unsigned wx) {
     Config::frozen = false;
@@ -129,6 +169,91 @@ void ref_patch_frame(const float* q, float* out) {
     out[0] = c.x; out[1] = c.y; out[2] = c.z;
     out[3] = n.x; out[4] = n.y; out[5] = n.z;
     out[6] = u.x; out[7] = u.y; out[8] = u.z;
+}
+
+// Display neighbours of the reference scene (after ref_scene_build), N x 8 scene indices.
+void ref_neighbours(unsigned* nb) { neighbours_of(g_scene, nb); }
+
+// Sets every patch's radiosity and illumination (N*3 each) and writes
+// Colors::smoothShadePatch of every patch (N*12), as the display update does.
+void ref_smooth_shade(const float* rad, const float* illum, float* colors) {
+    unsigned n = g_scene->getPatchesCount();
+    Patch** p = g_scene->getPatches();
+    for (unsigned i = 0; i < n; i++) {
+        p[i]->radiosity = Vector3f(rad[3 * i], rad[3 * i + 1], rad[3 * i + 2]);
+        p[i]->illumination = Vector3f(illum[3 * i], illum[3 * i + 1], illum[3 * i + 2]);
+    }
+    for (unsigned i = 0; i < n; i++) Colors::smoothShadePatch(colors + 12 * i, p[i]);
+}
+
+// Sets every patch's radiosity and returns getHighestRadiosityPatchId.
+unsigned ref_highest_id(const float* rad) {
+    unsigned n = g_scene->getPatchesCount();
+    Patch** p = g_scene->getPatches();
+    for (unsigned i = 0; i < n; i++) p[i]->radiosity = Vector3f(rad[3 * i], rad[3 * i + 1], rad[3 * i + 2]);
+    return g_scene->getHighestRadiosityPatchId();
+}
+
+// Loads an OBJ file through WaveFrontModel into a container subdivided to `area`;
+// returns the patch count.
+unsigned ref_obj_build(const char* path, double area) {
+    delete g_obj;
+    g_obj = new ModelContainer();
+    g_obj->maxPatchArea = area;
+    g_obj->addModel(new WaveFrontModel(path));
+    return g_obj->getPatchesCount();
+}
+
+void ref_obj_get(float* vertices, float* color, float* rad, float* illum, unsigned* nb) {
+    export_of(g_obj, vertices, color, rad, illum);
+    if (nb) neighbours_of(g_obj, nb);
+}
+
+// SaveToFile's file contents for the reference scene with the given state: a 32-bit
+// patch count (MSVC's unsigned long), then the Patch array with relative neighbours and
+// NULL neighbour pointers, as raw bytes.  Returns the bytes written (out may be NULL to
+// get the size); *record = sizeof(Patch) of this build.
+unsigned long long ref_rr_save(const float* rad, const float* illum, unsigned char* out, unsigned* record) {
+    unsigned n = g_scene->getPatchesCount();
+    Patch** patches = g_scene->getPatches();
+    *record = (unsigned)sizeof(Patch);
+    unsigned long long bytes = 4 + (unsigned long long)n * sizeof(Patch);
+    if (!out) return bytes;
+    for (unsigned i = 0; i < n; i++) {
+        patches[i]->radiosity = Vector3f(rad[3 * i], rad[3 * i + 1], rad[3 * i + 2]);
+        patches[i]->illumination = Vector3f(illum[3 * i], illum[3 * i + 1], illum[3 * i + 2]);
+    }
+    Patch* data = new Patch[n];
+    std::memset((void*)data, 0, sizeof(Patch) * n);  // padding bytes are otherwise indeterminate
+    for (unsigned long i = 0; i < n; i++) data[i] = (*patches[i]);
+    for (unsigned long i = 0; i < n; i++)
+        for (unsigned int k = 0; k < 8; k++)
+            for (unsigned long j = 0; j < n; j++)
+                if (patches[i]->neighbours[k] == patches[j]) {
+                    data[i].relativeNeighbours[k] = j;
+                    data[i].neighbours[k] = NULL;
+                    break;
+                }
+    const unsigned count = n;
+    std::memcpy(out, &count, 4);
+    std::memcpy(out + 4, (const void*)data, sizeof(Patch) * n);
+    delete[] data;
+    return bytes;
+}
+
+// LoadFromFile on file bytes of this build's Patch layout: a LoadingModel in a new
+// container (no subdivision).  Returns the patch count; ref_obj_get reads the result.
+unsigned ref_rr_load(const unsigned char* bytes) {
+    unsigned count;
+    std::memcpy(&count, bytes, 4);
+    Patch* data = new Patch[count];
+    std::memcpy((void*)data, bytes + 4, sizeof(Patch) * count);
+    delete g_obj;
+    g_obj = new ModelContainer();
+    g_obj->maxPatchArea = 0;
+    g_obj->addModel(new LoadingModel(data, count));
+    delete[] data;
+    return g_obj->getPatchesCount();
 }
 
 }  // extern "C"

@@ -36,6 +36,9 @@ EXPORTS = [
     "rad_dense_rows", "rad_gather_solve", "rad_gather_residual", "rad_shoot_residual", "rad_bf16_gemm", "rad_mlp_create", "rad_mlp_destroy",
     "rad_mlp_param_count", "rad_mlp_get_params", "rad_mlp_set_params", "rad_mlp_predict", "rad_mlp_gradients",
     "rad_mlp_train", "rad_multi_create", "rad_multi_shoot", "rad_multi_destroy", "rad_strerror", "rad_last_error",
+    "rad_scene_reference_neighbours", "rad_scene_obj", "rad_rr_size", "rad_rr_write", "rad_rr_read",
+    "rad_upload_neighbours", "rad_display_colors", "rad_display_colors_device", "rad_highest_patch", "rad_progress",
+    "rad_set_progress",
 ]
 STAGES = ["select", "camera", "setup", "bins", "raster", "update", "emitters"]
 STAGE_KERNELS = [1, 1, 1, 2, 1, 1, 1]
@@ -149,6 +152,19 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rad_raster_counters.argtypes = [vp, np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")]
     L.rad_reduce_items_noalloc.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp, vp]
     L.rad_scene_reference.argtypes = [ctypes.c_double, ctypes.c_uint32, P(ctypes.c_uint32), vp, vp, vp, vp, vp]
+    L.rad_scene_reference_neighbours.argtypes = [ctypes.c_double, ctypes.c_uint32, P(ctypes.c_uint32), vp]
+    L.rad_scene_obj.argtypes = [ctypes.c_char_p, ctypes.c_uint64, ctypes.c_double, ctypes.c_uint32,
+                                P(ctypes.c_uint32), vp, vp, vp, vp, vp, vp]
+    L.rad_rr_size.argtypes = [ctypes.c_uint32, ctypes.c_uint32, P(ctypes.c_uint64)]
+    L.rad_rr_write.argtypes = [ctypes.c_uint32, vp, vp, vp, vp, vp, ctypes.c_uint32, vp, ctypes.c_uint64]
+    L.rad_rr_read.argtypes = [vp, ctypes.c_uint64, ctypes.c_uint32, P(ctypes.c_uint32), vp, vp, vp, vp, vp, vp,
+                              P(ctypes.c_uint32)]
+    L.rad_upload_neighbours.argtypes = [vp, _u32p]
+    L.rad_display_colors.argtypes = [vp, vp, vp]
+    L.rad_display_colors_device.argtypes = [vp, vp, vp]
+    L.rad_highest_patch.argtypes = [vp, P(ctypes.c_uint32)]
+    L.rad_progress.argtypes = [vp, P(ctypes.c_uint32), P(ctypes.c_double)]
+    L.rad_set_progress.argtypes = [vp, ctypes.c_uint32, ctypes.c_double]
     L.rad_strerror.argtypes = [ctypes.c_int]
     L.rad_strerror.restype = ctypes.c_char_p
     L.rad_last_error.argtypes = [vp]
@@ -187,6 +203,85 @@ def reference_scene(max_patch_area: float) -> dict:
     if rc:
         raise RadError(rc, "rad_scene_reference")
     out["n"] = N
+    return out
+
+
+def _scene_arrays(N: int, neighbours: bool = True) -> dict:
+    out = dict(vertices=np.zeros(12 * N, np.float32), indices=np.zeros(6 * N, np.int32),
+               color=np.zeros(3 * N, np.float32), radiosity=np.zeros(3 * N, np.float32),
+               illumination=np.zeros(3 * N, np.float32))
+    if neighbours:
+        out["neighbours"] = np.zeros(8 * N, np.uint32)
+    return out
+
+
+def reference_neighbours(max_patch_area: float) -> np.ndarray:
+    """rad_scene_reference_neighbours: N x 8 display neighbours of the reference scene."""
+    L = load()
+    n = ctypes.c_uint32(0)
+    rc = L.rad_scene_reference_neighbours(max_patch_area, 0, ctypes.byref(n), None)
+    if rc:
+        raise RadError(rc, "rad_scene_reference_neighbours")
+    nb = np.zeros(8 * n.value, np.uint32)
+    rc = L.rad_scene_reference_neighbours(max_patch_area, n.value, ctypes.byref(n), _ptr(nb))
+    if rc:
+        raise RadError(rc, "rad_scene_reference_neighbours")
+    return nb
+
+
+def obj_scene(text: bytes, max_patch_area: float = 0.0) -> dict:
+    """rad_scene_obj: quads of a Wavefront OBJ file (bytes), subdivided to max_patch_area."""
+    L = load()
+    n = ctypes.c_uint32(0)
+    rc = L.rad_scene_obj(text, len(text), max_patch_area, 0, ctypes.byref(n), None, None, None, None, None, None)
+    if rc:
+        raise RadError(rc, "rad_scene_obj")
+    out = _scene_arrays(n.value)
+    rc = L.rad_scene_obj(text, len(text), max_patch_area, n.value, ctypes.byref(n), _ptr(out["vertices"]),
+                         _ptr(out["indices"]), _ptr(out["color"]), _ptr(out["radiosity"]), _ptr(out["illumination"]),
+                         _ptr(out["neighbours"]))
+    if rc:
+        raise RadError(rc, "rad_scene_obj")
+    out["n"] = n.value
+    return out
+
+
+def rr_write(vertices, color, radiosity, illumination, neighbours=None, pointer_bytes: int = 8) -> bytes:
+    """rad_rr_write: the reference's .rr scene file (SaveToFile) as bytes."""
+    L = load()
+    v = np.ascontiguousarray(vertices, np.float32)
+    n = v.size // 12
+    arrs = [np.ascontiguousarray(a, np.float32) for a in (color, radiosity, illumination)]
+    nb = None if neighbours is None else np.ascontiguousarray(neighbours, np.uint32)
+    size = ctypes.c_uint64(0)
+    rc = L.rad_rr_size(n, pointer_bytes, ctypes.byref(size))
+    if rc:
+        raise RadError(rc, "rad_rr_size")
+    buf = np.zeros(size.value, np.uint8)
+    rc = L.rad_rr_write(n, _ptr(v), _ptr(arrs[0]), _ptr(arrs[1]), _ptr(arrs[2]), _ptr(nb), pointer_bytes, _ptr(buf),
+                        size.value)
+    if rc:
+        raise RadError(rc, "rad_rr_write")
+    return buf.tobytes()
+
+
+def rr_read(data: bytes) -> dict:
+    """rad_rr_read: the scene of a .rr file (LoadFromFile + LoadingModel)."""
+    L = load()
+    raw = np.frombuffer(data, np.uint8)
+    n = ctypes.c_uint32(0)
+    ptr = ctypes.c_uint32(0)
+    rc = L.rad_rr_read(_ptr(raw), raw.size, 0, ctypes.byref(n), None, None, None, None, None, None, ctypes.byref(ptr))
+    if rc:
+        raise RadError(rc, "rad_rr_read")
+    out = _scene_arrays(n.value)
+    rc = L.rad_rr_read(_ptr(raw), raw.size, n.value, ctypes.byref(n), _ptr(out["vertices"]), _ptr(out["indices"]),
+                       _ptr(out["color"]), _ptr(out["radiosity"]), _ptr(out["illumination"]), _ptr(out["neighbours"]),
+                       ctypes.byref(ptr))
+    if rc:
+        raise RadError(rc, "rad_rr_read")
+    out["n"] = n.value
+    out["pointer_bytes"] = ptr.value
     return out
 
 
@@ -282,6 +377,34 @@ class Solver:
         i = np.zeros(3 * self.n, np.float32)
         self._check(self.L.rad_download(self.h, _ptr(r), _ptr(i)), "rad_download")
         return r, i
+
+    def upload_neighbours(self, neighbours):
+        """rad_upload_neighbours: N x 8 display neighbours for display_colors."""
+        nb = np.ascontiguousarray(neighbours, np.uint32).reshape(-1)
+        self._check(self.L.rad_upload_neighbours(self.h, nb), "rad_upload_neighbours")
+
+    def display_colors(self, colors: bool = True, radiative: bool = True):
+        """rad_display_colors: smoothShadePatch corner colours and corner radiosities (N x 12 each)."""
+        c = np.zeros(12 * self.n, np.float32) if colors else None
+        r = np.zeros(12 * self.n, np.float32) if radiative else None
+        self._check(self.L.rad_display_colors(self.h, _ptr(c), _ptr(r)), "rad_display_colors")
+        return c, r
+
+    def highest_patch(self) -> int:
+        """rad_highest_patch: getHighestRadiosityPatchId on the device state."""
+        out = ctypes.c_uint32(0)
+        self._check(self.L.rad_highest_patch(self.h, ctypes.byref(out)), "rad_highest_patch")
+        return out.value
+
+    def progress(self):
+        """rad_progress: (batches done, initial unshot power)."""
+        shots = ctypes.c_uint32(0)
+        p0 = ctypes.c_double(0)
+        self._check(self.L.rad_progress(self.h, ctypes.byref(shots), ctypes.byref(p0)), "rad_progress")
+        return shots.value, p0.value
+
+    def set_progress(self, shots_done: int, initial_power: float):
+        self._check(self.L.rad_set_progress(self.h, shots_done, initial_power), "rad_set_progress")
 
     def ff_table(self, copies: int = 1) -> np.ndarray:
         out = np.zeros(3 * self.W * self.W * copies, np.float32)

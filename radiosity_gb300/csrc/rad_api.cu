@@ -49,6 +49,9 @@ struct rad_ctx {
     float4* d_rad = nullptr;
     float4* d_illum = nullptr;
     float* d_area = nullptr;
+    uint32_t* d_nb = nullptr;      // display neighbours, N x 8 (rad_upload_neighbours)
+    float* d_shade = nullptr;      // display colour scratch, 2 x N x 12 (rad_display_colors)
+    unsigned long long* d_best = nullptr;  // argmax key (rad_highest_patch)
     float* d_fftab = nullptr;
     BinInfo* d_bins = nullptr;
     DevState* d_state = nullptr;   // shoot loop state
@@ -381,6 +384,9 @@ int rad_destroy(rad_ctx* c) {
     dfree(c->d_rad);
     dfree(c->d_illum);
     dfree(c->d_area);
+    dfree(c->d_nb);
+    dfree(c->d_shade);
+    dfree(c->d_best);
     dfree(c->d_fftab);
     dfree(c->d_bins);
     dfree(c->d_state);
@@ -433,6 +439,8 @@ int rad_upload_scene(rad_ctx* c, const float* vertices, const int32_t* indices, 
     dfree(c->d_rad);
     dfree(c->d_illum);
     dfree(c->d_area);
+    dfree(c->d_nb);
+    dfree(c->d_shade);
     c->n = n;
     c->geo.n = n;
     RAD_CUDA(c, cudaMalloc(&c->d_verts, sizeof(float) * 12 * (size_t)n));
@@ -1175,6 +1183,78 @@ int rad_multi_shoot(rad_multi* m, uint32_t n_replays, uint32_t* stop_replay, dou
     if (stop_ms) std::memcpy(stop_ms, at_ms.data(), sizeof(double) * count);
     if (replays) *replays = done_replays;
     if (device_ms) *device_ms = total;
+    return RAD_OK;
+}
+
+int rad_upload_neighbours(rad_ctx* c, const uint32_t* neighbours) {
+    if (!c) return RAD_E_INVALID;
+    if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
+    if (!neighbours) return fail(c, RAD_E_INVALID, "neighbours are required");
+    for (size_t i = 0; i < (size_t)c->n * 8; i++)
+        if (neighbours[i] >= c->n) return fail(c, RAD_E_INVALID, "neighbour index out of range");
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (!c->d_nb) RAD_CUDA(c, cudaMalloc(&c->d_nb, sizeof(uint32_t) * 8 * (size_t)c->n));
+    RAD_CUDA(c, cudaMemcpy(c->d_nb, neighbours, sizeof(uint32_t) * 8 * (size_t)c->n, cudaMemcpyHostToDevice));
+    return RAD_OK;
+}
+
+int rad_display_colors_device(rad_ctx* c, float* d_colors, float* d_radiative) {
+    if (!c) return RAD_E_INVALID;
+    if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
+    if (d_colors && !c->d_nb) return fail(c, RAD_E_STATE, "no neighbours uploaded");
+    if (!d_colors && !d_radiative) return RAD_OK;
+    launch_shade(c->n, c->d_nb, c->d_color, c->d_rad, c->d_illum, d_colors, d_radiative, c->stream);
+    RAD_CUDA(c, cudaGetLastError());
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    return RAD_OK;
+}
+
+int rad_display_colors(rad_ctx* c, float* colors, float* radiative) {
+    if (!c) return RAD_E_INVALID;
+    if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
+    if (colors && !c->d_nb) return fail(c, RAD_E_STATE, "no neighbours uploaded");
+    if (!colors && !radiative) return RAD_OK;
+    const size_t per = 12 * (size_t)c->n;
+    if (!c->d_shade) RAD_CUDA(c, cudaMalloc(&c->d_shade, sizeof(float) * 2 * per));
+    int rc = rad_display_colors_device(c, colors ? c->d_shade : nullptr, radiative ? c->d_shade + per : nullptr);
+    if (rc) return rc;
+    if (colors) RAD_CUDA(c, cudaMemcpy(colors, c->d_shade, sizeof(float) * per, cudaMemcpyDeviceToHost));
+    if (radiative) RAD_CUDA(c, cudaMemcpy(radiative, c->d_shade + per, sizeof(float) * per, cudaMemcpyDeviceToHost));
+    return RAD_OK;
+}
+
+int rad_highest_patch(rad_ctx* c, uint32_t* id) {
+    if (!c || !id) return RAD_E_INVALID;
+    if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
+    if (!c->d_best) RAD_CUDA(c, cudaMalloc(&c->d_best, sizeof(unsigned long long)));
+    RAD_CUDA(c, cudaMemsetAsync(c->d_best, 0, sizeof(unsigned long long), c->stream));
+    launch_argmax(c->n, c->cfg.mode == RAD_MODE_PHYS, c->d_rad, c->d_area, c->d_best, c->stream);
+    RAD_CUDA(c, cudaGetLastError());
+    unsigned long long best = 0;
+    RAD_CUDA(c, cudaMemcpyAsync(&best, c->d_best, sizeof(best), cudaMemcpyDeviceToHost, c->stream));
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    *id = best == ~0ull ? 0u : ~(uint32_t)(best & 0xFFFFFFFFull);
+    return RAD_OK;
+}
+
+int rad_progress(rad_ctx* c, uint32_t* shots_done, double* initial_power) {
+    if (!c) return RAD_E_INVALID;
+    if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
+    DevState st;
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    RAD_CUDA(c, cudaMemcpy(&st, c->d_state, sizeof(st), cudaMemcpyDeviceToHost));
+    if (shots_done) *shots_done = st.shots_done;
+    if (initial_power) *initial_power = st.power0;
+    return RAD_OK;
+}
+
+int rad_set_progress(rad_ctx* c, uint32_t shots_done, double initial_power) {
+    if (!c) return RAD_E_INVALID;
+    if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
+    if (!(initial_power >= 0)) return fail(c, RAD_E_INVALID, "initial power must be >= 0");
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    RAD_CUDA(c, cudaMemcpy(&c->d_state->shots_done, &shots_done, sizeof(shots_done), cudaMemcpyHostToDevice));
+    RAD_CUDA(c, cudaMemcpy(&c->d_state->power0, &initial_power, sizeof(initial_power), cudaMemcpyHostToDevice));
     return RAD_OK;
 }
 

@@ -133,6 +133,11 @@ void launch_update(const Geo& g, const Batch& b, const float4* color, const floa
 void launch_emitters(const Geo& g, const Batch& b, float4* rad, float4* illum, const float* area,
                      double tol, double* partials, DevState* st, cudaStream_t s);
 void launch_areas(const float* verts, uint32_t n, float* area, cudaStream_t s);
+// display.cu
+void launch_shade(uint32_t n, const uint32_t* nb, const float4* color, const float4* rad, const float4* illum,
+                  float* colors, float* radiative, cudaStream_t s);
+void launch_argmax(uint32_t n, bool phys, const float4* rad, const float* area, unsigned long long* best,
+                   cudaStream_t s);
 
 // dense.cu
 }  // namespace rad
