@@ -8,10 +8,17 @@
 //     scene.shoot(Config::SHOOTS_PER_CYCLE());           // GPU: select, render, reduce, update
 //     Patch** p = scene.getPatches();                    // radiosity / illumination synced back
 // Differences from the reference: Patch objects are host copies refreshed by shoot();
-// writing Patch::radiosity and calling scene.pushState() uploads edits.
+// writing Patch::radiosity and calling scene.pushState() uploads edits.  The display
+// update of source/Main.cpp:1318-1372 is scene.updateDisplayColors(colors, radiative)
+// (all patches at once on the GPU, Colors::smoothShadePatch per patch); SaveToFile /
+// LoadFromFile (source/Main.cpp:1460-1647) are scene.saveToFile(path) /
+// scene.loadFromFile(path) without the file dialogs; scene.loadObj(path) adds a
+// WaveFrontModel (source/WaveFrontModel.cpp:15-143) instead of the built-in scene.
 #pragma once
 #include <cstdint>
 #include <cstdio>
+#include <fstream>
+#include <iterator>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -94,8 +101,10 @@ inline float* precomputeHemicubeFormFactors() {
 class Patch {
   public:
     Vector3f radiosity, illumination;
+    Patch* neighbours[8] = {};  // display neighbours, numbered from the upper left corner (source/Patch.h:50)
     Vector3f getColor() const { return color; }
     float getReflectivity() const { return 0.3f; }  // REFLECTIVITY, source/Patch.h:13
+    Patch** getNeighbours() { return neighbours; }
     Vector3f color;
 };
 
@@ -125,6 +134,63 @@ class ModelContainer {
             p_emitters_ids[i] = v ? ids[i] : 0;
             p_emitters[i] = v ? patches[ids[i]] : nullptr;
         }
+    }
+    // getHighestRadiosityPatchId (source/ModelContainer.cpp:222-237) on the device state.
+    unsigned getHighestRadiosityPatchId() {
+        device();
+        uint32_t id = 0;
+        check(rad_highest_patch(ctx, &id));
+        return id;
+    }
+    // The display update after a batch of shots: colors = smoothShadePatch of every patch,
+    // radiative = radiosity at the 4 corners (N*12 floats each, the VBO layout).
+    void updateDisplayColors(std::vector<float>& colors, std::vector<float>& radiative) {
+        device();
+        colors.resize(12 * patches.size());
+        radiative.resize(12 * patches.size());
+        check(rad_display_colors(ctx, colors.data(), radiative.data()));
+    }
+    // SaveToFile without the dialog: the .rr file of this build's pointer width.
+    void saveToFile(const char* path) {
+        refresh();
+        std::vector<float> r(3 * patches.size()), il(3 * patches.size());
+        for (size_t i = 0; i < patches.size(); i++) {
+            r[3 * i] = patches[i]->radiosity.x; r[3 * i + 1] = patches[i]->radiosity.y; r[3 * i + 2] = patches[i]->radiosity.z;
+            il[3 * i] = patches[i]->illumination.x; il[3 * i + 1] = patches[i]->illumination.y;
+            il[3 * i + 2] = patches[i]->illumination.z;
+        }
+        uint64_t bytes = 0;
+        const uint32_t ptr = (uint32_t)sizeof(void*);
+        check(rad_rr_size((uint32_t)patches.size(), ptr, &bytes));
+        std::vector<unsigned char> buf((size_t)bytes);
+        check(rad_rr_write((uint32_t)patches.size(), vertices.data(), color.data(), r.data(), il.data(),
+                           neighbours.data(), ptr, buf.data(), bytes));
+        std::ofstream f(path, std::ios::binary);
+        f.write(reinterpret_cast<const char*>(buf.data()), (std::streamsize)buf.size());
+        if (!f) throw std::runtime_error("radiosity: unable to write the file");
+    }
+    // LoadFromFile without the dialog: replaces the scene by the file's patches.
+    void loadFromFile(const char* path) {
+        std::ifstream f(path, std::ios::binary);
+        std::vector<unsigned char> buf((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+        uint32_t n = 0, ptr = 0;
+        check(rad_rr_read(buf.data(), buf.size(), 0, &n, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, &ptr));
+        resize(n);
+        check(rad_rr_read(buf.data(), buf.size(), n, &n, vertices.data(), indices.data(), color.data(),
+                          radiosity0.data(), illumination0.data(), neighbours.data(), &ptr));
+        rebuild();
+    }
+    // A WaveFrontModel subdivided to maxPatchArea in place of the built-in scene.
+    void loadObj(const char* path) {
+        std::ifstream f(path, std::ios::binary);
+        std::string text((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+        uint32_t n = 0;
+        check(rad_scene_obj(text.data(), text.size(), maxPatchArea, 0, &n, nullptr, nullptr, nullptr, nullptr, nullptr,
+                            nullptr));
+        resize(n);
+        check(rad_scene_obj(text.data(), text.size(), maxPatchArea, n, &n, vertices.data(), indices.data(),
+                            color.data(), radiosity0.data(), illumination0.data(), neighbours.data()));
+        rebuild();
     }
     // `shots` iterations of the shoot loop; returns true when the stop rule fired.
     bool shoot(unsigned shots, rad_stats* stats = nullptr) {
@@ -159,30 +225,47 @@ class ModelContainer {
     rad_ctx* ctx = nullptr;
     std::vector<float> vertices, color, radiosity0, illumination0;
     std::vector<int> indices;
+    std::vector<uint32_t> neighbours;
     std::vector<Patch*> patches;
 
     void check(int rc) {
         if (rc != RAD_OK) throw std::runtime_error(std::string("radiosity: ") + rad_last_error(ctx));
     }
-    void refresh() {
-        if (!loaded || built) return;
-        uint32_t n = 0;
-        rad_scene_reference(maxPatchArea, 0, &n, nullptr, nullptr, nullptr, nullptr, nullptr);
+    void resize(uint32_t n) {
         vertices.resize(12 * (size_t)n);
         indices.resize(6 * (size_t)n);
         color.resize(3 * (size_t)n);
         radiosity0.resize(3 * (size_t)n);
         illumination0.resize(3 * (size_t)n);
-        rad_scene_reference(maxPatchArea, n, &n, vertices.data(), indices.data(), color.data(), radiosity0.data(),
-                            illumination0.data());
-        for (uint32_t i = 0; i < n; i++) {
+        neighbours.resize(8 * (size_t)n);
+    }
+    // Patch objects from the flat arrays (a new scene: any device context is dropped).
+    void rebuild() {
+        if (ctx) rad_destroy(ctx);
+        ctx = nullptr;
+        for (Patch* p : patches) delete p;
+        patches.clear();
+        const size_t n = color.size() / 3;
+        for (size_t i = 0; i < n; i++) {
             Patch* p = new Patch();
             p->color = Vector3f(color[3 * i], color[3 * i + 1], color[3 * i + 2]);
             p->radiosity = Vector3f(radiosity0[3 * i], radiosity0[3 * i + 1], radiosity0[3 * i + 2]);
             p->illumination = Vector3f(illumination0[3 * i], illumination0[3 * i + 1], illumination0[3 * i + 2]);
             patches.push_back(p);
         }
-        built = true;
+        for (size_t i = 0; i < n; i++)
+            for (int j = 0; j < 8; j++) patches[i]->neighbours[j] = patches[neighbours[8 * i + j]];
+        loaded = built = true;
+    }
+    void refresh() {
+        if (!loaded || built) return;
+        uint32_t n = 0;
+        rad_scene_reference(maxPatchArea, 0, &n, nullptr, nullptr, nullptr, nullptr, nullptr);
+        resize(n);
+        rad_scene_reference(maxPatchArea, n, &n, vertices.data(), indices.data(), color.data(), radiosity0.data(),
+                            illumination0.data());
+        rad_scene_reference_neighbours(maxPatchArea, n, &n, neighbours.data());
+        rebuild();
     }
     void device() {
         refresh();
@@ -190,6 +273,7 @@ class ModelContainer {
         if (rad_create(&Config::cfg(), &ctx) != RAD_OK) throw std::runtime_error("rad_create failed");
         check(rad_upload_scene(ctx, vertices.data(), indices.data(), color.data(), nullptr, radiosity0.data(),
                                illumination0.data(), (uint32_t)patches.size()));
+        check(rad_upload_neighbours(ctx, neighbours.data()));
     }
 };
 
