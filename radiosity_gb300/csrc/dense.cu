@@ -70,8 +70,11 @@ void launch_dense_rows(unsigned long long* Fq, uint32_t count, uint32_t n, uint3
 
 // ---------------------------------------------------------------------------
 // FP32 residual GEMM: r[c][i] = E[c][i] + rho_i[c%3] * sum_j F[i][j] X[c][j] - X[c][i]
-// 64 (rows) x 64 (columns) tiles, 16-deep k slabs, 4x4 outputs per thread.
-// Column norms: nrm[c] += r^2 (FP64 atomics).
+// 64 (rows) x 64 (columns) tiles, 16-deep k slabs, 4x4 outputs per thread.  Each slab
+// is summed in FP32 and added to a (hi, lo) pair with Knuth's TwoSum, so the sum over
+// N ~ 20k terms carries the rounding of a 16-term slab instead of growing like
+// sqrt(N) * eps: the refinement's FP32 residual then agrees with an FP64 evaluation to
+// well below the 1e-6 tolerance.  Column norms: nrm[c] += r^2 (FP64 atomics).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_sgemm_resid(const float* __restrict__ F, uint32_t n, uint32_t ld,
                                                      const float* __restrict__ X, const float* __restrict__ E,
@@ -81,8 +84,9 @@ __global__ void __launch_bounds__(256) k_sgemm_resid(const float* __restrict__ F
     __shared__ float Bs[16][64 + 4];
     const uint32_t i0 = blockIdx.x * 64, c0 = blockIdx.y * 64;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    float acc[4][4] = {};
+    float hi[4][4] = {}, lo[4][4] = {};
     for (uint32_t k0 = 0; k0 < n; k0 += 16) {
+        float acc[4][4] = {};
         for (int e = threadIdx.x; e < 64 * 16; e += 256) {
             const int rr = e >> 4, kk = e & 15;
             const uint32_t gi = i0 + rr, gk = k0 + kk, gc = c0 + rr;
@@ -104,6 +108,15 @@ __global__ void __launch_bounds__(256) k_sgemm_resid(const float* __restrict__ F
                 for (int q = 0; q < 4; q++) acc[p][q] = fmaf(a[p], bb[q], acc[p][q]);
         }
         __syncthreads();
+#pragma unroll
+        for (int p = 0; p < 4; p++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) {  // TwoSum(hi, acc): s + e == hi + acc exactly
+                const float a = hi[p][q], b = acc[p][q];
+                const float s = a + b, bv = s - a;
+                lo[p][q] += (a - (s - bv)) + (b - bv);
+                hi[p][q] = s;
+            }
     }
 #pragma unroll
     for (int q = 0; q < 4; q++) {
@@ -117,7 +130,7 @@ __global__ void __launch_bounds__(256) k_sgemm_resid(const float* __restrict__ F
                 const float4 rh = rho[i];
                 const int ch = (int)(c % 3);
                 const float rr = ch == 0 ? rh.x : (ch == 1 ? rh.y : rh.z);
-                const float v = E[(size_t)c * n + i] + rr * acc[p][q] - X[(size_t)c * n + i];
+                const float v = E[(size_t)c * n + i] + rr * (hi[p][q] + lo[p][q]) - X[(size_t)c * n + i];
                 r[(size_t)c * n + i] = v;
                 part += (double)v * (double)v;
             }
