@@ -129,3 +129,21 @@ def test_checkpoint_resume_through_rr_file_is_bit_exact(lib, tmp_path, mode):
     assert np.array_equal(_bits(rad2), _bits(rad_full)) and np.array_equal(_bits(ill2), _bits(ill_full))
     if mode == 1:
         assert st.residual == full.residual
+
+
+def test_display_colors_into_caller_device_buffers(lib, sio):
+    torch = pytest.importorskip("torch")
+    import ctypes
+
+    sc = lib.reference_scene(0.5)
+    n = sc["n"]
+    rad, ill, want = sio["shade_rad"][0], sio["shade_illum"][0], sio["shade_colors"][0]
+    d_colors = torch.zeros(12 * n, dtype=torch.float32, device="cuda:0")
+    d_rad = torch.zeros(12 * n, dtype=torch.float32, device="cuda:0")
+    with solver(lib, sc) as s:
+        s.upload_neighbours(lib.reference_neighbours(0.5))
+        s.set_state(radiosity=rad, illumination=ill)
+        rc = s.L.rad_display_colors_device(s.h, ctypes.c_void_p(d_colors.data_ptr()), ctypes.c_void_p(d_rad.data_ptr()))
+        assert rc == 0
+    assert np.array_equal(_bits(d_colors.cpu().numpy()), _bits(want))
+    assert np.array_equal(_bits(d_rad.cpu().numpy()), _bits(np.tile(rad.reshape(-1, 1, 3), (1, 4, 1)).ravel()))
