@@ -1008,6 +1008,19 @@ __global__ void __launch_bounds__(256, 4) k_raster(Geo g, Batch b, const float* 
             __syncthreads();
         }
     }
+    // The reduction's delta form factors are loaded now, ahead of the barrier, so that
+    // their L2 latency overlaps the barrier and the hash-table clear (kSeg per thread,
+    // the column segment the thread walks below).
+    constexpr int kSeg = TILE * TILE / 256 > 4 ? TILE * TILE / 256 : 4;
+    constexpr int kWalkers = TILE * TILE / kSeg;
+    const int wx = threadIdx.x % TILE, wr0 = (threadIdx.x / TILE) * kSeg;
+    const bool walker = fused && valid && (int)threadIdx.x < kWalkers;
+    float ffv[kSeg];
+#pragma unroll
+    for (int i = 0; i < kSeg; i++) {
+        ffv[i] = 0.f;
+        if (walker && wx < bi.w && wr0 + i < bi.h) ffv[i] = fftab[(size_t)(bi.y0 + wr0 + i) * g.TW + bi.x0 + wx];
+    }
     __syncthreads();
     if (count && threadIdx.x < 8) {
         uint32_t v = s_cnt[threadIdx.x];
@@ -1035,26 +1048,22 @@ __global__ void __launch_bounds__(256, 4) k_raster(Geo g, Batch b, const float* 
     // Each thread walks kSeg consecutive pixels down one column of the bin, summing the
     // exact fixed-point delta form factors (ff * 2^61) while the patch id stays the same,
     // and adds each run's sum to the bin's id -> sum table once.  Lanes take adjacent
-    // columns, so key and table reads are conflict-free / coalesced.
-    constexpr int kSeg = TILE * TILE / 256 > 4 ? TILE * TILE / 256 : 4;
-    constexpr int kWalkers = TILE * TILE / kSeg;
-    if (valid && (int)threadIdx.x < kWalkers) {
-        const int x = threadIdx.x % TILE, r0 = (threadIdx.x / TILE) * kSeg;
-        const bool col_in = x < bi.w;
-        const float* ffcol = fftab + (size_t)(bi.y0 + r0) * g.TW + bi.x0 + x;
+    // columns, so key reads are conflict-free.
+    if (walker) {
+        const bool col_in = wx < bi.w;
         uint32_t cur = kHashEmpty;
         unsigned long long acc = 0;
-#pragma unroll 8
+#pragma unroll
         for (int i = 0; i < kSeg; i++) {
-            const unsigned long long k = key[(r0 + i) * TILE + x];
-            const bool has = col_in && r0 + i < bi.h && k != ~0ull;
+            const unsigned long long k = key[(wr0 + i) * TILE + wx];
+            const bool has = col_in && wr0 + i < bi.h && k != ~0ull;
             const uint32_t id = has ? (uint32_t)k : kHashEmpty;
             if (id != cur) {
                 if (cur != kHashEmpty) hash_add(h_id, h_sum, Fq, cur, acc);
                 cur = id;
                 acc = 0;
             }
-            if (has) acc += __float2ull_rz(ffcol[(size_t)i * g.TW] * 0x1p61f);
+            if (has) acc += __float2ull_rz(ffv[i] * 0x1p61f);
         }
         if (cur != kHashEmpty) hash_add(h_id, h_sum, Fq, cur, acc);
     }
