@@ -57,6 +57,7 @@ struct rad_ctx {
     DevState* d_state = nullptr;   // shoot loop state
     DevState* d_aux = nullptr;     // state for the one-off entry points
     uint32_t* h_flag = nullptr;    // pinned stop flag
+    float4* h_stage = nullptr;     // pinned staging for the state copies, 2 x N float4 (null: pageable path)
     BatchBuf shoot;                // K = hemicubes_count
     BatchBuf aux;                  // one-off calls, grown on demand
     float* d_rows = nullptr;       // float rows for ff_rows / reduce
@@ -396,6 +397,7 @@ int rad_destroy(rad_ctx* c) {
     dfree(c->d_F16);
     dfree(c->d_scale);
     if (c->h_flag) cudaFreeHost(c->h_flag);
+    if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -455,6 +457,12 @@ int rad_upload_scene(rad_ctx* c, const float* vertices, const int32_t* indices, 
     if ((rc = upload_f3(c, c->d_rho, reflectance, n))) return rc;
     if ((rc = upload_f3(c, c->d_rad, radiosity, n))) return rc;
     if ((rc = upload_f3(c, c->d_illum, illumination, n))) return rc;
+    if (c->h_stage) cudaFreeHost(c->h_stage);
+    c->h_stage = nullptr;
+    if (cudaMallocHost(&c->h_stage, sizeof(float4) * 2 * (size_t)n) != cudaSuccess) {
+        c->h_stage = nullptr;  // the state copies then go through pageable memory
+        cudaGetLastError();
+    }
     launch_areas(c->d_verts, n, c->d_area, c->stream);
     RAD_CUDA(c, cudaMemsetAsync(c->d_state, 0, sizeof(DevState), c->stream));
     launch_power0(c->d_rad, c->d_area, n, c->d_state, c->stream);
@@ -467,29 +475,47 @@ int rad_upload_scene(rad_ctx* c, const float* vertices, const int32_t* indices, 
 int rad_set_state(rad_ctx* c, const float* radiosity, const float* illumination) {
     if (!c) return RAD_E_INVALID;
     if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
-    cudaStreamSynchronize(c->stream);
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    const size_t n = c->n;
     int rc;
-    if (radiosity && (rc = upload_f3(c, c->d_rad, radiosity, c->n))) return rc;
-    if (illumination && (rc = upload_f3(c, c->d_illum, illumination, c->n))) return rc;
-    uint32_t zero = 0;
-    RAD_CUDA(c, cudaMemcpy(&c->d_state->stopped, &zero, sizeof(zero), cudaMemcpyHostToDevice));
+    if (c->h_stage) {  // pack into pinned memory, two asynchronous copies, one wait
+        const float* src[2] = {radiosity, illumination};
+        float4* dst[2] = {c->d_rad, c->d_illum};
+        for (int k = 0; k < 2; k++) {
+            if (!src[k]) continue;
+            float4* st = c->h_stage + k * n;
+            for (size_t i = 0; i < n; i++) st[i] = make_float4(src[k][3 * i], src[k][3 * i + 1], src[k][3 * i + 2], 0.f);
+            RAD_CUDA(c, cudaMemcpyAsync(dst[k], st, sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream));
+        }
+    } else {
+        if (radiosity && (rc = upload_f3(c, c->d_rad, radiosity, c->n))) return rc;
+        if (illumination && (rc = upload_f3(c, c->d_illum, illumination, c->n))) return rc;
+    }
+    RAD_CUDA(c, cudaMemsetAsync(&c->d_state->stopped, 0, sizeof(uint32_t), c->stream));
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
     return RAD_OK;
 }
 
 int rad_download(rad_ctx* c, float* radiosity, float* illumination) {
     if (!c) return RAD_E_INVALID;
     if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
-    std::vector<float4> tmp(c->n);
-    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    const size_t n = c->n;
     float* dst[2] = {radiosity, illumination};
     float4* src[2] = {c->d_rad, c->d_illum};
+    std::vector<float4> tmp;
+    if (!c->h_stage) tmp.resize(2 * n);
+    float4* stage = c->h_stage ? c->h_stage : tmp.data();
+    for (int k = 0; k < 2; k++)
+        if (dst[k])
+            RAD_CUDA(c, cudaMemcpyAsync(stage + k * n, src[k], sizeof(float4) * n, cudaMemcpyDeviceToHost, c->stream));
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
     for (int k = 0; k < 2; k++) {
         if (!dst[k]) continue;
-        RAD_CUDA(c, cudaMemcpy(tmp.data(), src[k], sizeof(float4) * c->n, cudaMemcpyDeviceToHost));
-        for (uint32_t i = 0; i < c->n; i++) {
-            dst[k][3 * i] = tmp[i].x;
-            dst[k][3 * i + 1] = tmp[i].y;
-            dst[k][3 * i + 2] = tmp[i].z;
+        const float4* st = stage + k * n;
+        for (size_t i = 0; i < n; i++) {
+            dst[k][3 * i] = st[i].x;
+            dst[k][3 * i + 1] = st[i].y;
+            dst[k][3 * i + 2] = st[i].z;
         }
     }
     return RAD_OK;
