@@ -738,10 +738,12 @@ __device__ __forceinline__ void raster_small(const RQuad& t, int x0, int x1, int
     for (int i = 0; i < steps; i++) {
         const int32_t ca = f[0] | f[1] | f[2], cb = f[3] | f[4] | f[5];
         if ((ca & cb) >= 0) {
+            // one plane per lane (A when inside A, else B), so the warp evaluates one depth
+            const bool ina = ca >= 0;
+            const float c0 = ina ? c0a : c0b, ax = ina ? axa : axb, ay = ina ? aya : ayb;
             const float u = (float)(px - sx), wv = (float)(py - sy);
-            unsigned long long k = ~0ull;
-            if (ca >= 0) k = ((unsigned long long)depth_ordinal((c0a + axa * u) + aya * wv) << 32) | id;
-            if (cb >= 0) {
+            unsigned long long k = ((unsigned long long)depth_ordinal((c0 + ax * u) + ay * wv) << 32) | id;
+            if (ina && cb >= 0) {  // inside both (a folded outline): the smaller of the two keys
                 const unsigned long long kb = ((unsigned long long)depth_ordinal((c0b + axb * u) + ayb * wv) << 32) | id;
                 k = kb < k ? kb : k;
             }
