@@ -681,6 +681,17 @@ __device__ __forceinline__ int block_exclusive_scan(int v, uint32_t* ws) {
     return (int)ws[warp] + x - v;
 }
 
+// 64-bit add as two native 32-bit shared atomics: the low word first, its carry into the
+// high word.  Every add commutes, so the final 64-bit value is the exact sum; the table is
+// read only after a barrier.
+__device__ __forceinline__ void shared_add64(unsigned long long* p, unsigned long long v) {
+    uint32_t* w = reinterpret_cast<uint32_t*>(p);  // w[0] = low word, w[1] = high word
+    const uint32_t lo = (uint32_t)v, hi = (uint32_t)(v >> 32);
+    const uint32_t old = atomicAdd(&w[0], lo);
+    const uint32_t up = hi + ((uint32_t)(old + lo) < old ? 1u : 0u);
+    if (up) atomicAdd(&w[1], up);
+}
+
 // Adds an exact partial sum to the bin's open-addressing id -> sum table (linear probing,
 // at most 32 probes); a crowded table sends the sum straight to the global row.
 __device__ __forceinline__ void hash_add(uint32_t* h_id, unsigned long long* h_sum, unsigned long long* Fq,
@@ -693,7 +704,7 @@ __device__ __forceinline__ void hash_add(uint32_t* h_id, unsigned long long* h_s
             if (cur == kHashEmpty) cur = id;
         }
         if (cur == id) {
-            atomicAdd(&h_sum[slot], sum);
+            shared_add64(&h_sum[slot], sum);
             return;
         }
         slot = (slot + 1) & (kHashSlots - 1);
