@@ -420,8 +420,21 @@ __global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* _
         }
         if (!behind)
             for (int f = 0; f < 5; f++) {
+                // the z and w rows first: all four corners outside the near plane
+                // (z + w < 0) reject the face without the x and y rows; the rows are the
+                // same float expressions as face_corners', so the mask is unchanged
+                const float* mm = s_mvp + f * 16;
+                bool near_out = true;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const float x = q[3 * k], y = q[3 * k + 1], z = q[3 * k + 2];
+                    const float cz = ((mm[2] * x + mm[6] * y) + mm[10] * z) + mm[14];
+                    const float cw = ((mm[3] * x + mm[7] * y) + mm[11] * z) + mm[15];
+                    if (!(cz + cw < 0)) near_out = false;
+                }
+                if (near_out) continue;
                 float4 cv[4];
-                if (face_corners(q, s_mvp + f * 16, f, cv)) mask |= 1u << f;
+                if (face_corners(q, mm, f, cv)) mask |= 1u << f;
             }
     }
     // 2. compaction
