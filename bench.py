@@ -151,8 +151,8 @@ def ncu_traffic(k: int):
 def sm_side_ncu():
     """k_raster's SM-side figures from profiles/k_raster_k_setup_full_room50k_w512_k8.md."""
     return {"source": "profiles/k_raster_k_setup_full_room50k_w512_k8.md (ncu --set full, K=8)",
-            "issue_slots_busy_frac": 0.517, "shared_pipe_frac": 0.525, "sm_throughput_frac": 0.378,
-            "active_lanes_per_warp_instruction": 21.4, "dram_throughput_frac": 0.018}
+            "issue_slots_busy_frac": 0.536, "shared_pipe_frac": 0.594, "sm_throughput_frac": 0.382,
+            "active_lanes_per_warp_instruction": 24.6, "dram_throughput_frac": 0.022}
 
 
 def cpu_baseline(sc, W, K, seconds):
