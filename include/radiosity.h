@@ -18,7 +18,7 @@ extern "C" {
 #define RAD_OK 0
 #define RAD_E_INVALID (-1)  /* bad argument (reference: cerr + ignore, source/Config.cpp:54-112) */
 #define RAD_E_CUDA (-2)     /* CUDA runtime error (reference: _ASSERT on CL calls) */
-#define RAD_E_OVERFLOW (-3) /* triangle or bin capacity exceeded; results of the call invalid */
+#define RAD_E_OVERFLOW (-3) /* raster record or bin capacity exceeded; results of the call invalid */
 #define RAD_E_STATE (-4)    /* call out of order (e.g. no scene uploaded) */
 #define RAD_E_NOMEM (-5)    /* device allocation failed */
 #define RAD_E_TIMEOUT (-6)  /* a bounded device wait gave up */
@@ -36,10 +36,11 @@ typedef struct rad_config {
     uint32_t mode;            /* rad_mode: REF = the reference's update rule, PHYS = rho*F*Ai/Aj */
     uint32_t tile;            /* raster bin side in pixels: 16, 32 or 64; 0 = choose by W */
     double tolerance;         /* PHYS stop rule: unshot power / initial power <= tolerance */
-    uint32_t tri_capacity;    /* triangle records per hemicube; 0 = 2*N + 4096 */
+    uint32_t tri_capacity;    /* raster records per hemicube (one per patch quad and face, up to 4 per
+                                 clipped quad); 0 = 3*N + 4096 */
     uint32_t binref_capacity; /* bin references per hemicube; 0 = 4 * tri_capacity */
     int32_t device;           /* CUDA device ordinal */
-    uint32_t small_tri_pixels;/* triangles whose clamped bin area is at most this many pixels (and whose
+    uint32_t small_tri_pixels;/* records whose box clamped to a bin is at most this many pixels (and whose
                                  extent is at most 64 px) are rasterised by one lane; 0 = 64 */
 } rad_config;
 
@@ -113,7 +114,7 @@ int rad_shoot(rad_ctx* ctx, uint32_t n_shots, rad_stats* stats);
 /* Stages of one shoot batch, in launch order (rad_profile_stages). */
 #define RAD_STAGE_SELECT 0   /* shooter selection (1 kernel) */
 #define RAD_STAGE_CAMERA 1   /* face MVPs + saved energy (1 kernel) */
-#define RAD_STAGE_SETUP 2    /* triangle setup + bin counts (1 kernel) */
+#define RAD_STAGE_SETUP 2    /* raster record setup + bin counts (1 kernel) */
 #define RAD_STAGE_BINS 3     /* bin scan + fill (2 kernels) */
 #define RAD_STAGE_RASTER 4   /* tile raster + fused delta-FF reduction (1 kernel) */
 #define RAD_STAGE_UPDATE 5   /* radiosity update (1 kernel) */
@@ -225,9 +226,10 @@ int rad_multi_shoot(rad_multi* m, uint32_t n_replays, uint32_t* stop_replay, dou
                     double* device_ms);
 int rad_multi_destroy(rad_multi* m);
 
-/* Raster counters of the last rad_profile_stages call (8 values): triangle-bin pairs,
- * small triangles (one lane each), their bbox pixels, large triangles (one warp each),
- * their 8x4 stamps, stamps visited, stamps wholly inside, large-triangle pixels written. */
+/* Raster counters of the last rad_profile_stages call (8 values): record-bin pairs (a record
+ * holds both triangles of a patch quad), small records (one lane each), their box pixels,
+ * big records (one warp per triangle), their 8x4 stamps, stamps visited, stamps wholly
+ * inside, big-triangle pixels written. */
 int rad_raster_counters(rad_ctx* ctx, uint64_t* out);
 
 /* Builds the reference scene (ModelContainer::load, source/ModelContainer.cpp:89-110,

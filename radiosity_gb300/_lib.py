@@ -493,8 +493,8 @@ class Solver:
                     "rad_shoot_residual")
         return r
 
-    RASTER_COUNTERS = ["pairs", "small_tris", "small_px", "big_tris", "big_stamps", "stamps_visited",
-                       "stamps_inside", "big_px_written"]
+    RASTER_COUNTERS = ["record_bin_pairs", "small_records", "small_box_px", "big_records", "big_stamps",
+                       "stamps_visited", "stamps_inside", "big_px_written"]
 
     def raster_counters(self) -> dict:
         out = np.zeros(8, np.uint64)

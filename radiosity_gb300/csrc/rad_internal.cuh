@@ -81,8 +81,8 @@ struct DevState {
     double hemicubes;
     uint32_t timeouts;
     uint32_t pad[3];
-    // raster counters (filled when counting is on): tri-bin pairs, small tris, small bbox px,
-    // big tris, big stamps in bbox, stamps visited, stamps fully inside, big pixels plotted
+    // raster counters (filled when counting is on): record-bin pairs, small records, small box px,
+    // big records, big stamps in bbox, stamps visited, stamps fully inside, big pixels plotted
     unsigned long long raster_counters[8];
 };
 

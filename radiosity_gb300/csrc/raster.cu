@@ -5,18 +5,21 @@
 // kernel (source/Kernel_ProcessHemicube.h:9-70) with a sort-middle tile
 // rasteriser:
 //   k_camera   K*5 face MVPs + shooter frame + saved unshot energy
-//   k_setup    thread per (hemicube, patch): shooter-plane cull, clip-space
-//              transform, trivial frustum/scissor reject, near/far/guard clip,
-//              fixed-point snap, back-face cull; emits 64-byte triangle records
-//              (warp-aggregated allocation) and counts per-bin references
+//   k_setup    thread per (hemicube, patch): shooter-plane cull, exact per-face
+//              mask, clip-space transform, near/far/guard clip, fixed-point snap,
+//              back-face cull; emits one 64-byte record per patch quad and face
+//              (both triangles; warp-aggregated allocation) and counts per-bin
+//              references
 //   k_scan     exclusive scan of the bin counts
-//   k_fill     scatters triangle ids into per-bin lists
+//   k_fill     scatters record indices into per-bin lists
 //   k_raster   CTA per (hemicube, tile x tile bin): depth|id keys in shared memory
-//              (atomicMin = GL_LESS with patch-index draw order), then either the
-//              uint32 item buffer or the fused reduction: each pixel's delta FF is
-//              an exact multiple of 2^-61, lanes with equal ids are grouped with
-//              __match_any_sync, summed exactly with three redux.sync partial sums,
-//              and one 64-bit atomicAdd per (warp, id) lands in Fq[hemicube][id].
+//              (atomicMin = GL_LESS with patch-index draw order), small records one
+//              lane each, big triangles one warp each; then either the uint32 item
+//              buffer or the fused reduction: each pixel's delta FF is an exact
+//              multiple of 2^-61, summed per run of equal ids down each column into
+//              a per-bin id -> sum table, flushed with one 64-bit atomicAdd per id
+//              into Fq[hemicube][id].  k_reduce_items does the same for caller item
+//              buffers with __match_any_sync groups and exact redux.sync sums.
 // The raster rules are spelled out in oracle/oracle.h (the CPU restatement the
 // parity tests compare against bit for bit).
 #include <cuda_runtime.h>

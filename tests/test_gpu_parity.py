@@ -276,7 +276,7 @@ def test_lane_warp_split_is_exact(lib, orc, cornell, small):
         F = s.ff_rows(sh)
         s.profile_stages(1)
         c = s.raster_counters()
-    assert c["pairs"] > 0 and c["small_tris"] + c["big_tris"] <= c["pairs"]
+    assert c["record_bin_pairs"] > 0 and c["small_records"] + c["big_records"] <= c["record_bin_pairs"]
     items = np.concatenate([orc.render(W, cornell["vertices"], int(p)) for p in sh])
     assert np.array_equal(_bits(F), _bits(orc.ff_exact(W, items, len(sh), n)))
 
