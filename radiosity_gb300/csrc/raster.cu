@@ -398,6 +398,8 @@ __global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* _
     __shared__ float s_mvp[5 * 16];
     __shared__ float s_fr[8];
     __shared__ uint8_t s_items[4][32 * 5];  // (lane << 3) | face
+    __shared__ uint32_t s_clipq[128 * 5];   // items that need clipping: (patch << 3) | face
+    __shared__ uint32_t s_nclip;
     // per-CTA bin histogram (when the hemicube has <= kSetupHistBins bins): shared-memory
     // atomics per triangle, one global add per touched bin at the end
     extern __shared__ uint32_t s_hist[];
@@ -406,6 +408,7 @@ __global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* _
     uint32_t* cnt = use_hist ? s_hist : gcnt;
     for (int i = threadIdx.x; i < 5 * 16; i += blockDim.x) s_mvp[i] = b.mvp[(size_t)hi * 80 + i];
     if (threadIdx.x < 8) s_fr[threadIdx.x] = b.frame[(size_t)hi * 8 + threadIdx.x];
+    if (threadIdx.x == 0) s_nclip = 0;
     if (use_hist)
         for (uint32_t i = threadIdx.x; i < g.nb; i += blockDim.x) s_hist[i] = 0;
     __syncthreads();
@@ -456,7 +459,10 @@ __global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* _
             if ((mask >> f) & 1u) items[k++] = (uint8_t)((lane << 3) | (uint32_t)f);
     }
     __syncwarp();
-    // 3. items, 32 at a time
+    // 3. items, 32 at a time.  An item whose four corners need no clipping is one record
+    //    (both triangles).  Items that need clipping (a few percent, but enough to put
+    //    one in about half of all 32-item groups) are queued and clipped afterwards in
+    //    compact groups, so the common path does not wait for them.
     const uint32_t pbase = blockIdx.x * blockDim.x + warp * 32;
     for (uint32_t r = 0; r < total; r += 32) {
         const bool has = r + lane < total;
@@ -474,48 +480,68 @@ __global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* _
             load_quad(verts, pp, q);
             face_corners(q, s_mvp + f * 16, f, cv);
         }
-        const float hw = 0.5f * (float)F.vp[2], hh = 0.5f * (float)F.vp[3];
-        const float vx = (float)F.vp[0], vy = (float)F.vp[1];
-        // an item whose four corners need no clipping is one record (both triangles);
-        // otherwise each triangle is clipped and its fan packed two triangles per record
         const bool clipq =
             has && (needs_clip(cv[0]) || needs_clip(cv[1]) || needs_clip(cv[2]) || needs_clip(cv[3]));
-        const bool anyclip = __any_sync(0xffffffffu, clipq);
-        for (int t = 0; t < (anyclip ? 2 : 1); t++) {  // warp-uniform trip count
-            SV s[4];
-            int pa[4], pb[4], px[4];
-            bool okA = false, okB = false;
-            if (has && !clipq && t == 0) {
-                const bool g0 = snap_vertex(cv[0], hw, hh, vx, vy, s[0]), g1 = snap_vertex(cv[1], hw, hh, vx, vy, s[1]);
-                const bool g2 = snap_vertex(cv[2], hw, hh, vx, vy, s[2]), g3 = snap_vertex(cv[3], hw, hh, vx, vy, s[3]);
-                okA = g0 && g1 && g2 && tri_bbox(s[0], s[1], s[2], F, pa);
-                okB = g0 && g2 && g3 && tri_bbox(s[0], s[2], s[3], F, pb);
-            }
+        const uint32_t qpos = warp_alloc(&s_nclip, clipq ? 1u : 0u);
+        if (clipq) s_clipq[qpos] = (pp << 3) | (uint32_t)f;
+        SV sv[4];
+        int pa[4], pb[4], px[4];
+        bool okA = false, okB = false;
+        if (has && !clipq) {
+            const float hw = 0.5f * (float)F.vp[2], hh = 0.5f * (float)F.vp[3];
+            const float vx = (float)F.vp[0], vy = (float)F.vp[1];
+            const bool g0 = snap_vertex(cv[0], hw, hh, vx, vy, sv[0]), g1 = snap_vertex(cv[1], hw, hh, vx, vy, sv[1]);
+            const bool g2 = snap_vertex(cv[2], hw, hh, vx, vy, sv[2]), g3 = snap_vertex(cv[3], hw, hh, vx, vy, sv[3]);
+            okA = g0 && g1 && g2 && tri_bbox(sv[0], sv[1], sv[2], F, pa);
+            okB = g0 && g2 && g3 && tri_bbox(sv[0], sv[2], sv[3], F, pb);
+        }
+        const bool quad = okA || okB;
+        // slots are allocated per hemicube (one counter each, not one for the batch)
+        const uint32_t base = warp_alloc(&b.tri_counts[hi], quad ? 1u : 0u);
+        const bool written = quad && base < b.tri_cap_h;
+        if (quad) {
+            if (!written) atomicOr(&st->overflow, 1u);
+            else rec_write(sv, okA, okB, pa, pb, pp, f, &b.tris[(size_t)hi * b.tri_cap_h + base]);
+            box_union(okA, okB, pa, pb, px);
+        }
+        if (use_hist) {
+            if (written) count_bins(g, F, px, cnt);
+        } else {
+            count_bins_warp(g, b, hi, F, px, written);
+        }
+    }
+    // queued clip items, 32 per warp: each triangle is clipped and its fan packed two
+    // triangles per record
+    __syncthreads();
+    const uint32_t nclip = s_nclip;
+    for (uint32_t r = warp * 32; r < nclip; r += blockDim.x) {  // warp-uniform trip count
+        const bool has = r + lane < nclip;
+        uint32_t pp = 0;
+        int f = 0;
+        float4 cv[4];
+        if (has) {
+            const uint32_t it = s_clipq[r + lane];
+            pp = it >> 3;
+            f = (int)(it & 7u);
+            float q[12];
+            load_quad(verts, pp, q);
+            face_corners(q, s_mvp + f * 16, f, cv);
+        }
+        const FaceInfo& F = g.face[f];
+        const float hw = 0.5f * (float)F.vp[2], hh = 0.5f * (float)F.vp[3];
+        const float vx = (float)F.vp[0], vy = (float)F.vp[1];
+        for (int t = 0; t < 2; t++) {
             float4 poly[12];
             int pn = 0;
-            if (clipq) {
+            if (has) {
                 poly[0] = cv[0];
                 poly[1] = cv[1 + t];
                 poly[2] = cv[2 + t];
                 pn = clip_polygon(poly, 3);
             }
-            const bool quad = okA || okB;
-            const uint32_t ncand = quad ? 1u : fan_records(pn);
-            // slots are allocated per hemicube (one counter each, not one for the batch)
+            const uint32_t ncand = fan_records(pn);
             const uint32_t base = warp_alloc(&b.tri_counts[hi], ncand);
-            const bool written = quad && base < b.tri_cap_h;
-            if (quad) {
-                if (!written) atomicOr(&st->overflow, 1u);
-                else rec_write(s, okA, okB, pa, pb, pp, f, &b.tris[(size_t)hi * b.tri_cap_h + base]);
-                box_union(okA, okB, pa, pb, px);
-            } else if (ncand) {
-                emit_polygon(g, b, poly, pn, base, pp, hi, f, hw, hh, vx, vy, cnt, st);
-            }
-            if (use_hist) {
-                if (written) count_bins(g, F, px, cnt);
-            } else {
-                count_bins_warp(g, b, hi, F, px, written);
-            }
+            if (ncand) emit_polygon(g, b, poly, pn, base, pp, hi, f, hw, hh, vx, vy, cnt, st);  // counts its bins
         }
     }
     if (use_hist) {
