@@ -429,39 +429,42 @@ __global__ void __launch_bounds__(256) k_update(Geo g, Batch b, const float4* __
     __syncthreads();
     const uint32_t N = g.n;
     double acc = 0;
+    // The hemicubes' contributions are added in hemicube order (the float sums must match
+    // the oracle's order); their exact sums are loaded kLoad at a time ahead of use, so a
+    // thread keeps several independent loads in flight instead of one.
+    constexpr int kLoad = 8;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
         float4 r = rad[i];
-        if (g.mode == 0) {
-            for (int h = 0; h < K; h++) {
-                if (!s_valid[h]) continue;
-                unsigned long long* fq = b.Fq + (size_t)h * N + i;
-                const unsigned long long q = *fq;
-                if (q == 0) continue;
-                *fq = 0;
-                const float F = __ull2float_rn(q) * 0x1p-61f;
-                const float4 s = s_saved[h], c = s_col[h];
-                float t;
-                t = s.x * F; t = t * kReflectivity; t = t * c.x; r.x = r.x + t;
-                t = s.y * F; t = t * kReflectivity; t = t * c.y; r.y = r.y + t;
-                t = s.z * F; t = t * kReflectivity; t = t * c.z; r.z = r.z + t;
+        const float ai = g.mode ? area[i] : 0.f;
+        const float4 rh = g.mode ? rho[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int h0 = 0; h0 < K; h0 += kLoad) {
+            unsigned long long qv[kLoad];
+#pragma unroll
+            for (int j = 0; j < kLoad; j++) {
+                const int h = h0 + j;
+                qv[j] = (h < K && s_valid[h]) ? b.Fq[(size_t)h * N + i] : 0ull;
             }
-        } else {
-            const float ai = area[i];
-            const float4 rh = rho[i];
-            for (int h = 0; h < K; h++) {
-                if (!s_valid[h]) continue;
-                unsigned long long* fq = b.Fq + (size_t)h * N + i;
-                const unsigned long long q = *fq;
+#pragma unroll
+            for (int j = 0; j < kLoad; j++) {
+                const unsigned long long q = qv[j];
                 if (q == 0) continue;
-                *fq = 0;
-                if (!(ai > 0)) continue;
+                const int h = h0 + j;
+                b.Fq[(size_t)h * N + i] = 0;  // ready for the next batch
                 const float F = __ull2float_rn(q) * 0x1p-61f;
-                const float gg = (F * s_area[h]) / ai;
-                const float4 s = s_saved[h];
+                const float4 sv = s_saved[h];
                 float t;
-                t = s.x * gg; t = rh.x * t; r.x = r.x + t;
-                t = s.y * gg; t = rh.y * t; r.y = r.y + t;
-                t = s.z * gg; t = rh.z * t; r.z = r.z + t;
+                if (g.mode == 0) {  // source/Main.cpp:1274, REFLECTIVITY and the shooter's colour
+                    const float4 c = s_col[h];
+                    t = sv.x * F; t = t * kReflectivity; t = t * c.x; r.x = r.x + t;
+                    t = sv.y * F; t = t * kReflectivity; t = t * c.y; r.y = r.y + t;
+                    t = sv.z * F; t = t * kReflectivity; t = t * c.z; r.z = r.z + t;
+                } else {
+                    if (!(ai > 0)) continue;
+                    const float gg = (F * s_area[h]) / ai;
+                    t = sv.x * gg; t = rh.x * t; r.x = r.x + t;
+                    t = sv.y * gg; t = rh.y * t; r.y = r.y + t;
+                    t = sv.z * gg; t = rh.z * t; r.z = r.z + t;
+                }
             }
         }
         rad[i] = r;
