@@ -560,30 +560,55 @@ void launch_setup(const Geo& g, const Batch& b, const float* verts, DevState* st
 // ---------------------------------------------------------------------------
 // Bin lists
 // ---------------------------------------------------------------------------
+// Exclusive scan of the K * nb bin counts by one CTA in tiles of 4096: each thread takes 4
+// consecutive counts (coalesced), warps scan with shuffles, a carry links the tiles.  Also
+// clears the fill cursors and flags a bin-list overflow.
 __global__ void __launch_bounds__(1024) k_scan(Geo g, Batch b, DevState* st) {
     if (st->stopped) return;
     const uint32_t total = b.K * g.nb;
-    const uint32_t tid = threadIdx.x, nt = blockDim.x;
-    const uint32_t per = (total + nt - 1) / nt;
-    const uint32_t lo = tid * per, hi = min(total, lo + per);
-    uint32_t s = 0;
-    for (uint32_t i = lo; i < hi; i++) s += b.bin_count[i];
-    __shared__ uint32_t part[1024];
-    part[tid] = s;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_carry;
+    if (tid == 0) s_carry = 0;
     __syncthreads();
-    for (uint32_t o = 1; o < nt; o <<= 1) {
-        uint32_t v = tid >= o ? part[tid - o] : 0;
+    for (uint32_t base = 0; base < total; base += 4 * blockDim.x) {
+        const uint32_t i0 = base + 4 * tid;
+        uint32_t c[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) c[k] = i0 + k < total ? b.bin_count[i0 + k] : 0u;
+        const uint32_t t4 = (c[0] + c[1]) + (c[2] + c[3]);
+        uint32_t x = t4;  // inclusive warp scan of the threads' 4-count totals
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane == 31) s_warp[warp] = x;
         __syncthreads();
-        part[tid] += v;
+        if (warp == 0) {
+            uint32_t w = lane < (blockDim.x >> 5) ? s_warp[lane] : 0u;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= (uint32_t)o) w += y;
+            }
+            s_warp[lane] = w;  // inclusive over warps
+        }
+        __syncthreads();
+        uint32_t run = s_carry + (warp ? s_warp[warp - 1] : 0u) + (x - t4);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (i0 + k < total) {
+                b.bin_offset[i0 + k] = run;
+                b.bin_fill[i0 + k] = 0;
+            }
+            run += c[k];
+        }
+        __syncthreads();
+        if (tid == blockDim.x - 1) s_carry = run;  // the tile's end
         __syncthreads();
     }
-    uint32_t run = part[tid] - s;
-    for (uint32_t i = lo; i < hi; i++) {
-        b.bin_offset[i] = run;
-        b.bin_fill[i] = 0;
-        run += b.bin_count[i];
-    }
-    if (tid == nt - 1 && part[tid] > b.list_cap) atomicOr(&st->overflow, 2u);
+    if (tid == 0 && s_carry > b.list_cap) atomicOr(&st->overflow, 2u);
 }
 
 __global__ void k_fill(Geo g, Batch b, DevState* st) {
