@@ -70,65 +70,92 @@ void launch_dense_rows(unsigned long long* Fq, uint32_t count, uint32_t n, uint3
 
 // ---------------------------------------------------------------------------
 // FP32 residual GEMM: r[c][i] = E[c][i] + rho_i[c%3] * sum_j F[i][j] X[c][j] - X[c][i]
-// 64 (rows) x 64 (columns) tiles, 16-deep k slabs, 4x4 outputs per thread.  Each slab
-// is summed in FP32 and added to a (hi, lo) pair with Knuth's TwoSum, so the sum over
-// N ~ 20k terms carries the rounding of a 16-term slab instead of growing like
-// sqrt(N) * eps: the refinement's FP32 residual then agrees with an FP64 evaluation to
-// well below the 1e-6 tolerance.  Column norms: nrm[c] += r^2 (FP64 atomics).
+// 128 (rows) x 64 (columns) tiles, 16-deep k slabs staged in shared memory (the next
+// slab's global loads are issued before the current slab's FMAs), 8x4 outputs per thread.
+// Every 64 k the FP32 partial sums are added to a (hi, lo) pair with Knuth's TwoSum, so the
+// sum over N ~ 20k terms carries the rounding of 64-term partials instead of growing like
+// sqrt(N) * eps: the refinement's FP32 residual then agrees with an FP64 evaluation to well
+// below the 1e-6 tolerance.  Column norms: nrm[c] += r^2 (FP64 atomics).  Entries of F at
+// columns >= n (the row padding up to ld) are never read as data.
 // ---------------------------------------------------------------------------
+constexpr int kRBM = 128, kRBN = 64, kRBK = 16, kRComp = 4;  // kRComp slabs between TwoSums
+
 __global__ void __launch_bounds__(256) k_sgemm_resid(const float* __restrict__ F, uint32_t n, uint32_t ld,
                                                      const float* __restrict__ X, const float* __restrict__ E,
                                                      const float4* __restrict__ rho, uint32_t R, float* r,
                                                      double* nrm) {
-    __shared__ float As[16][64 + 4];
-    __shared__ float Bs[16][64 + 4];
-    const uint32_t i0 = blockIdx.x * 64, c0 = blockIdx.y * 64;
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    float hi[4][4] = {}, lo[4][4] = {};
-    for (uint32_t k0 = 0; k0 < n; k0 += 16) {
-        float acc[4][4] = {};
-        for (int e = threadIdx.x; e < 64 * 16; e += 256) {
-            const int rr = e >> 4, kk = e & 15;
-            const uint32_t gi = i0 + rr, gk = k0 + kk, gc = c0 + rr;
-            As[kk][rr] = (gi < n && gk < n) ? F[(size_t)gi * ld + gk] : 0.f;
-            Bs[kk][rr] = (gc < R && gk < n) ? X[(size_t)gc * n + gk] : 0.f;
+    __shared__ __align__(16) float As[kRBK][kRBM + 4];  // As[k][i]
+    __shared__ __align__(16) float Bs[kRBK][kRBN + 4];  // Bs[k][c]
+    const uint32_t i0 = blockIdx.x * kRBM, c0 = blockIdx.y * kRBN;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    // global -> register staging: A: row tid/2, 8 consecutive k; B: column tid/4, 4 consecutive k
+    const int ar = tid >> 1, ak = (tid & 1) * 8, bc = tid >> 2, bk = (tid & 3) * 4;
+    const uint32_t gi = i0 + ar, gc = c0 + bc;
+    float ra[8], rb[4];
+    auto load = [&](uint32_t k0) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const uint32_t gk = k0 + ak + j;
+            ra[j] = (gi < n && gk < n) ? F[(size_t)gi * ld + gk] : 0.f;
         }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const uint32_t gk = k0 + bk + j;
+            rb[j] = (gc < R && gk < n) ? X[(size_t)gc * n + gk] : 0.f;
+        }
+    };
+    float acc[8][4], hi[8][4], lo[8][4];
+#pragma unroll
+    for (int p = 0; p < 8; p++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) acc[p][q] = hi[p][q] = lo[p][q] = 0.f;
+    load(0);
+    int slab = 0;
+    for (uint32_t k0 = 0; k0 < n; k0 += kRBK) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) As[ak + j][ar] = ra[j];
+#pragma unroll
+        for (int j = 0; j < 4; j++) Bs[bk + j][bc] = rb[j];
         __syncthreads();
+        if (k0 + kRBK < n) load(k0 + kRBK);  // in flight during the FMAs below
 #pragma unroll
-        for (int kk = 0; kk < 16; kk++) {
-            float a[4], bb[4];
+        for (int kk = 0; kk < kRBK; kk++) {
+            const float4 a0 = *reinterpret_cast<const float4*>(&As[kk][ty * 8]);
+            const float4 a1 = *reinterpret_cast<const float4*>(&As[kk][ty * 8 + 4]);
+            const float4 b4 = *reinterpret_cast<const float4*>(&Bs[kk][tx * 4]);
+            const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float bb[4] = {b4.x, b4.y, b4.z, b4.w};
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                a[q] = As[kk][ty * 4 + q];
-                bb[q] = Bs[kk][tx * 4 + q];
-            }
-#pragma unroll
-            for (int p = 0; p < 4; p++)
+            for (int p = 0; p < 8; p++)
 #pragma unroll
                 for (int q = 0; q < 4; q++) acc[p][q] = fmaf(a[p], bb[q], acc[p][q]);
         }
         __syncthreads();
+        if (++slab == kRComp || k0 + kRBK >= n) {
+            slab = 0;
 #pragma unroll
-        for (int p = 0; p < 4; p++)
+            for (int p = 0; p < 8; p++)
 #pragma unroll
-            for (int q = 0; q < 4; q++) {  // TwoSum(hi, acc): s + e == hi + acc exactly
-                const float a = hi[p][q], b = acc[p][q];
-                const float s = a + b, bv = s - a;
-                lo[p][q] += (a - (s - bv)) + (b - bv);
-                hi[p][q] = s;
-            }
+                for (int q = 0; q < 4; q++) {  // TwoSum(hi, acc): s + e == hi + acc exactly
+                    const float a = hi[p][q], b = acc[p][q];
+                    const float s = a + b, bv = s - a;
+                    lo[p][q] += (a - (s - bv)) + (b - bv);
+                    hi[p][q] = s;
+                    acc[p][q] = 0.f;
+                }
+        }
     }
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         const uint32_t c = c0 + tx * 4 + q;
         double part = 0;
         if (c < R) {
+            const int ch = (int)(c % 3);
 #pragma unroll
-            for (int p = 0; p < 4; p++) {
-                const uint32_t i = i0 + ty * 4 + p;
+            for (int p = 0; p < 8; p++) {
+                const uint32_t i = i0 + ty * 8 + p;
                 if (i >= n) continue;
                 const float4 rh = rho[i];
-                const int ch = (int)(c % 3);
                 const float rr = ch == 0 ? rh.x : (ch == 1 ? rh.y : rh.z);
                 const float v = E[(size_t)c * n + i] + rr * (hi[p][q] + lo[p][q]) - X[(size_t)c * n + i];
                 r[(size_t)c * n + i] = v;
@@ -141,7 +168,7 @@ __global__ void __launch_bounds__(256) k_sgemm_resid(const float* __restrict__ F
 
 void launch_sgemm_resid(const float* F, uint32_t n, uint32_t ld, const float* X, const float* E, const float4* rho,
                         uint32_t R, float* r, double* nrm, cudaStream_t s) {
-    dim3 grid((n + 63) / 64, (R + 63) / 64);
+    dim3 grid((n + kRBM - 1) / kRBM, (R + kRBN - 1) / kRBN);
     k_sgemm_resid<<<grid, 256, 0, s>>>(F, n, ld, X, E, rho, R, r, nrm);
 }
 
