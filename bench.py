@@ -417,7 +417,7 @@ def run_precision(args):
             "gather": {"outer": st.outer, "sweeps": st.sweeps, "initial_residual": st.initial_residual,
                        "residual": st.residual, "sweep_ms": st.sweep_ms, "resid_ms": st.resid_ms},
             "fp64_residual_max": float(res.max()),
-            "roofline": {"kernel": "k_gemm_tc (tcgen05 BF16 sweep, fused epilogue)", "bound": "hbm",
+            "roofline": {"kernel": "k_gemm_tc + k_tc_finalize (tcgen05 BF16 sweep, deterministic split-K)", "bound": "hbm",
                          "achieved": gbs, "peak": float(peaks["hbm_gbs"]), "unit": "GB/s",
                          "frac": gbs / float(peaks["hbm_gbs"]), "tensor_tflops": tf,
                          "tensor_frac": tf / float(peaks["bf16_tflops"])},

@@ -15,12 +15,16 @@
 // transposed operand into a 4-stage ring, warp 1 issues tcgen05.mma (BF16 x BF16 ->
 // FP32 in TMEM) and frees stages with tcgen05.commit, warp 2 owns the TMEM
 // allocation, and warps 4-7 read the accumulator with tcgen05.ld and run the fused
-// epilogue.  Every mbarrier wait is bounded by wall-clock time; a timeout sets the
+// epilogue.  When the row tiles alone would leave SMs idle (160 tiles on 152 SMs at
+// N = 20k), K is split over blockIdx.y; each split writes its FP32 partial sums and
+// k_tc_finalize adds them in split order (deterministic) before the same epilogue.  Every mbarrier wait is bounded by wall-clock time; a timeout sets the
 // error word and the kernel drains and frees its TMEM before returning.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <cmath>
 
 #include "rad_internal.cuh"
 
@@ -344,6 +348,9 @@ __global__ void __launch_bounds__(256, 1) k_gemm_tc(const __grid_constant__ CUte
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t m0 = blockIdx.x * kTcM;
+    // split-K: block (x, y) takes K blocks [kb0, kb1) of split y
+    const uint32_t nsplit = (ep.partial && ep.ksplit > 1) ? ep.ksplit : 1u, split = blockIdx.y;
+    const uint32_t kb0 = split * kblocks / nsplit, kb1 = (split + 1) * kblocks / nsplit;
     if (threadIdx.x == 0) {
         for (int s = 0; s < kTcStages; s++) {
             mbar_init(&full[s], 1);
@@ -363,8 +370,8 @@ __global__ void __launch_bounds__(256, 1) k_gemm_tc(const __grid_constant__ CUte
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t taddr = *tmem_slot;
     if (warp == 0 && lane == 0) {
-        for (uint32_t kb = 0; kb < kblocks; kb++) {
-            const uint32_t s = kb % kTcStages, round = kb / kTcStages;
+        for (uint32_t kb = kb0; kb < kb1; kb++) {
+            const uint32_t s = (kb - kb0) % kTcStages, round = (kb - kb0) / kTcStages;
             if (!mbar_wait(&empty[s], (round & 1u) ^ 1u, ep.err)) break;
             mbar_expect_tx(&full[s], S::kStage);
             tma_load_2d(smem + s * S::kStage, &tmA, (int)(kb * kTcBK), (int)m0, &full[s]);
@@ -372,8 +379,8 @@ __global__ void __launch_bounds__(256, 1) k_gemm_tc(const __grid_constant__ CUte
         }
     } else if (warp == 1 && lane == 0) {
         bool ok = true;
-        for (uint32_t kb = 0; kb < kblocks; kb++) {
-            const uint32_t s = kb % kTcStages, round = kb / kTcStages;
+        for (uint32_t kb = kb0; kb < kb1; kb++) {
+            const uint32_t s = (kb - kb0) % kTcStages, round = (kb - kb0) / kTcStages;
             if (!mbar_wait(&full[s], round & 1u, ep.err)) {
                 ok = false;
                 break;
@@ -383,7 +390,7 @@ __global__ void __launch_bounds__(256, 1) k_gemm_tc(const __grid_constant__ CUte
             const uint64_t b0 = sw128_desc(smem_u32(smem + s * S::kStage + S::kA));
 #pragma unroll
             for (int k = 0; k < kTcBK / 16; k++) {
-                const uint32_t acc = (kb | (uint32_t)k) ? 1u : 0u;
+                const uint32_t acc = ((kb - kb0) | (uint32_t)k) ? 1u : 0u;
                 asm volatile(
                     "{ .reg .pred p; setp.ne.b32 p, %4, 0; tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(
                         taddr),
@@ -422,6 +429,15 @@ __global__ void __launch_bounds__(256, 1) k_gemm_tc(const __grid_constant__ CUte
                     : "r"(ta));
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 if (!live) continue;
+                if (nsplit > 1) {  // raw partial sums; k_tc_finalize adds the splits in order
+#pragma unroll
+                    for (int j = 0; j < 32; j++) {
+                        const uint32_t c = (uint32_t)(c0 + j);
+                        if (c >= ep.R) break;
+                        ep.partial[((size_t)split * ep.R + c) * ep.n + row] = __uint_as_float(v[j]);
+                    }
+                    continue;
+                }
 #pragma unroll
                 for (int j = 0; j < 32; j++) {
                     const uint32_t c = (uint32_t)(c0 + j);
@@ -476,6 +492,45 @@ static bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t l
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Split-K epilogue: y = scale * (sum of the splits' partial sums, in split order), then the
+// same update and BF16 copy as the fused epilogue.  Element (c, row) per thread.
+__global__ void k_tc_finalize(TcEpilogue ep) {
+    const size_t total = (size_t)ep.R * ep.n;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t c = (uint32_t)(e / ep.n), row = (uint32_t)(e % ep.n);
+        float acc = 0.f;
+        for (uint32_t sp = 0; sp < ep.ksplit; sp++) acc += ep.partial[((size_t)sp * ep.R + c) * ep.n + row];
+        const float sc = ep.scale ? ep.scale[row] : 1.0f;
+        float y = sc * acc;
+        if (ep.mode == 1) {
+            const float4 rh = ep.rho[row];
+            const int ch = (int)(c % 3);
+            const float rr = ch == 0 ? rh.x : (ch == 1 ? rh.y : rh.z);
+            y = ep.resid[(size_t)c * ep.n + row] + rr * y;
+        }
+        ep.out[(size_t)c * ep.n + row] = y;
+        if (ep.out16) ep.out16[(size_t)c * ep.ld16 + row] = __float2bfloat16_rn(y);
+    }
+}
+
+// K splits for n rows: the count (1..8, at least 8 K blocks each) that minimises
+// waves x (K blocks per split + a fixed per-block cost of 4 K blocks) on 152 SMs.
+uint32_t gemm_tc_ksplit(uint32_t n, uint32_t ld) {
+    const uint32_t tiles = (n + kTcM - 1) / kTcM, kblocks = ld / kTcBK;
+    uint32_t best = 1;
+    double best_cost = 1e300;
+    for (uint32_t sp = 1; sp <= 8; sp++) {
+        if (sp > 1 && kblocks / sp < 8) break;
+        const double waves = std::ceil((double)tiles * sp / 152.0);
+        const double cost = waves * ((double)kblocks / sp + 4.0);
+        if (cost < best_cost - 1e-9) {
+            best_cost = cost;
+            best = sp;
+        }
+    }
+    return best;
+}
+
 template <int NR>
 static int launch_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv_bfloat16* Bt, const TcEpilogue& ep,
                      cudaStream_t s) {
@@ -489,7 +544,9 @@ static int launch_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv
         attr = true;
     }
     const uint32_t kblocks = ld / kTcBK;
-    k_gemm_tc<NR><<<(n + kTcM - 1) / kTcM, 256, S::kSmem, s>>>(ma, mb, kblocks, ep);
+    const uint32_t nsplit = (ep.partial && ep.ksplit > 1) ? ep.ksplit : 1u;
+    k_gemm_tc<NR><<<dim3((n + kTcM - 1) / kTcM, nsplit), 256, S::kSmem, s>>>(ma, mb, kblocks, ep);
+    if (nsplit > 1) k_tc_finalize<<<152 * 8, 256, 0, s>>>(ep);
     return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 

@@ -893,14 +893,15 @@ int rad_gather_solve(rad_ctx* c, const float* emission, uint32_t R, const float*
     const uint32_t n = c->n, ld = c->dense_ld;
     const size_t nr = (size_t)n * R;
     cudaStream_t s = c->stream;
-    float *dE = nullptr, *dB = nullptr, *dr = nullptr, *dd = nullptr;
+    float *dE = nullptr, *dB = nullptr, *dr = nullptr, *dd = nullptr, *dpart = nullptr;
     __nv_bfloat16* d16[2] = {nullptr, nullptr};
+    const uint32_t ksplit = gemm_tc_ksplit(n, ld);
     double* dnrm = nullptr;
     uint32_t* derr = nullptr;
     int rc = RAD_OK;
     auto cleanup = [&]() {
         cudaFree(dE); cudaFree(dB); cudaFree(dr); cudaFree(dd);
-        cudaFree(d16[0]); cudaFree(d16[1]); cudaFree(dnrm); cudaFree(derr);
+        cudaFree(d16[0]); cudaFree(d16[1]); cudaFree(dnrm); cudaFree(derr); cudaFree(dpart);
     };
 #define G_CUDA(call)                                                                                  \
     do {                                                                                              \
@@ -918,6 +919,7 @@ int rad_gather_solve(rad_ctx* c, const float* emission, uint32_t R, const float*
     G_CUDA(cudaMalloc(&d16[0], 2 * (size_t)Rpad * ld));
     G_CUDA(cudaMalloc(&d16[1], 2 * (size_t)Rpad * ld));
     G_CUDA(cudaMalloc(&dnrm, 8 * (size_t)R));
+    if (ksplit > 1) G_CUDA(cudaMalloc(&dpart, 4 * nr * ksplit));
     G_CUDA(cudaMalloc(&derr, 4));
     G_CUDA(cudaMemsetAsync(derr, 0, 4, s));
     G_CUDA(cudaMemcpyAsync(dE, emission, 4 * nr, cudaMemcpyHostToDevice, s));
@@ -970,6 +972,8 @@ int rad_gather_solve(rad_ctx* c, const float* emission, uint32_t R, const float*
                 ep.out16 = d16[cur ^ 1];
                 ep.ld16 = ld;
                 ep.err = derr;
+                ep.partial = dpart;
+                ep.ksplit = ksplit;
                 if (launch_gemm_tc(c->d_F16, n, ld, d16[cur], Rpad, ep, s) != 0) {
                     cleanup();
                     return fail(c, RAD_E_CUDA, "tcgen05 GEMM launch failed");

@@ -153,6 +153,8 @@ struct TcEpilogue {
     __nv_bfloat16* out16;      // R x ld16 (next operand), may be null
     uint32_t ld16;
     uint32_t* err;
+    float* partial;            // split-K partial sums, ksplit x R x n (null: one split, fused epilogue)
+    uint32_t ksplit;           // K splits (gemm_tc_ksplit); > 1 only with `partial`
 };
 void launch_dense_rows(unsigned long long* Fq, uint32_t count, uint32_t n, uint32_t ld, uint32_t first,
                        float* F32, __nv_bfloat16* F16, float* scale, cudaStream_t s);
@@ -166,6 +168,7 @@ void launch_axpy(float* y, const float* x, size_t total, cudaStream_t s);
 int launch_gemm_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv_bfloat16* Bt, uint32_t Rpad,
                    const TcEpilogue& ep, cudaStream_t s);
 uint32_t gemm_tc_width(uint32_t R);
+uint32_t gemm_tc_ksplit(uint32_t n, uint32_t ld);  // K splits that fill the GPU best for n rows
 void launch_fftab(uint32_t W, float* fftab, cudaStream_t s);
 
 }  // namespace rad
