@@ -57,6 +57,7 @@ def parse():
     p.add_argument("--workload", default="large", choices=["large", "small", "precision", "learned", "uneven"],
                    help="large: the headline plain configuration; the others are the other benchmark configs")
     p.add_argument("--fp64-solve", action="store_true", help="precision: also solve the full system in FP64 on CPU")
+    p.add_argument("--precision-patches", type=int, default=20000, help="precision: patch count of the scene")
     p.add_argument("--uneven-tol", type=float, default=1e-4, help="uneven: unshot-fraction tolerance per scene")
     p.add_argument("--headline-patches", type=int, default=50000,
                    help="learned: patch count of the time-to-1e-4 comparison scene (0 skips it)")
@@ -389,7 +390,7 @@ def run_precision(args):
     import radiosity_gb300 as R
     from radiosity_gb300 import scenes
 
-    sc = scenes.cornell_box(target=20000)
+    sc = scenes.cornell_box(target=args.precision_patches)
     n, W = sc["n"], args.w
     s = R.Solver(hemicube_side=W, hemicubes_count=32, mode=R.MODE_PHYS)
     s.upload(sc["vertices"], sc["color"], sc["radiosity"], sc["illumination"], reflectance=sc["reflectance"])

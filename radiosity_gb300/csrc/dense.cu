@@ -513,16 +513,19 @@ __global__ void k_tc_finalize(TcEpilogue ep) {
     }
 }
 
-// K splits for n rows: the count (1..8, at least 8 K blocks each) that minimises
-// waves x (K blocks per split + a fixed per-block cost of 4 K blocks) on 152 SMs.
-uint32_t gemm_tc_ksplit(uint32_t n, uint32_t ld) {
+// K splits for n rows and R right-hand sides: the count (1..8, at least 8 K blocks each)
+// that minimises the bytes moved per row, with the F reads (2 ld bytes) divided by the
+// share of the 152 SMs the last wave keeps busy, plus the partial sums written and read
+// back (8 R bytes per split) when K is split.
+uint32_t gemm_tc_ksplit(uint32_t n, uint32_t ld, uint32_t R) {
     const uint32_t tiles = (n + kTcM - 1) / kTcM, kblocks = ld / kTcBK;
     uint32_t best = 1;
     double best_cost = 1e300;
     for (uint32_t sp = 1; sp <= 8; sp++) {
         if (sp > 1 && kblocks / sp < 8) break;
-        const double waves = std::ceil((double)tiles * sp / 152.0);
-        const double cost = waves * ((double)kblocks / sp + 4.0);
+        const double work = (double)tiles * sp;
+        const double fill = work / (std::ceil(work / 152.0) * 152.0);
+        const double cost = 2.0 * ld / fill + (sp > 1 ? 8.0 * R * sp : 0.0);
         if (cost < best_cost - 1e-9) {
             best_cost = cost;
             best = sp;

@@ -895,7 +895,7 @@ int rad_gather_solve(rad_ctx* c, const float* emission, uint32_t R, const float*
     cudaStream_t s = c->stream;
     float *dE = nullptr, *dB = nullptr, *dr = nullptr, *dd = nullptr, *dpart = nullptr;
     __nv_bfloat16* d16[2] = {nullptr, nullptr};
-    const uint32_t ksplit = gemm_tc_ksplit(n, ld);
+    const uint32_t ksplit = gemm_tc_ksplit(n, ld, Rpad);
     double* dnrm = nullptr;
     uint32_t* derr = nullptr;
     int rc = RAD_OK;

@@ -168,7 +168,7 @@ void launch_axpy(float* y, const float* x, size_t total, cudaStream_t s);
 int launch_gemm_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv_bfloat16* Bt, uint32_t Rpad,
                    const TcEpilogue& ep, cudaStream_t s);
 uint32_t gemm_tc_width(uint32_t R);
-uint32_t gemm_tc_ksplit(uint32_t n, uint32_t ld);  // K splits that fill the GPU best for n rows
+uint32_t gemm_tc_ksplit(uint32_t n, uint32_t ld, uint32_t R);  // K splits that fill the GPU best
 void launch_fftab(uint32_t W, float* fftab, cudaStream_t s);
 
 }  // namespace rad
