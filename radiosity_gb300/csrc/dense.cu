@@ -467,15 +467,17 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+// Looked up once; function-local static initialisation is thread-safe, so contexts driven
+// from several host threads share the lookup.
 static EncodeTiledFn encode_fn() {
-    static EncodeTiledFn fn = nullptr;
-    if (!fn) {
+    static const EncodeTiledFn fn = [] {
         void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeTiledFn>(p);
-    }
+            return reinterpret_cast<EncodeTiledFn>(p);
+        return EncodeTiledFn(nullptr);
+    }();
     return fn;
 }
 
@@ -540,12 +542,9 @@ static int launch_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv
     using S = TcShape<NR>;
     CUtensorMap ma, mb;
     if (!make_map(&ma, A, n, ld, kTcM) || !make_map(&mb, Bt, NR, ld, NR)) return -1;
-    static bool attr = false;
-    if (!attr) {
-        if (cudaFuncSetAttribute(k_gemm_tc<NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::kSmem) != cudaSuccess)
-            return -2;
-        attr = true;
-    }
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_gemm_tc<NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::kSmem);
+    if (attr != cudaSuccess) return -2;
     const uint32_t kblocks = ld / kTcBK;
     const uint32_t nsplit = (ep.partial && ep.ksplit > 1) ? ep.ksplit : 1u;
     k_gemm_tc<NR><<<dim3((n + kTcM - 1) / kTcM, nsplit), 256, S::kSmem, s>>>(ma, mb, kblocks, ep);
