@@ -60,7 +60,15 @@ def parse():
     p.add_argument("--precision-patches", type=int, default=20000, help="precision: patch count of the scene")
     p.add_argument("--uneven-tol", type=float, default=1e-4, help="uneven: unshot-fraction tolerance per scene")
     p.add_argument("--headline-patches", type=int, default=50000,
-                   help="learned: patch count of the time-to-1e-4 comparison scene (0 skips it)")
+                   help="patch count of the time-to-1e-4 comparison scene in the default line")
+    p.add_argument("--train-scenes", type=int, default=2000, help="learned: solver-generated training scenes")
+    p.add_argument("--train-patches", default="5000,50000", help="learned: training patch range (log-uniform)")
+    p.add_argument("--train-sample", type=int, default=2048, help="learned: patches kept per training scene")
+    p.add_argument("--train-epochs", type=int, default=50, help="learned: training epochs")
+    p.add_argument("--eval-scenes", type=int, default=100, help="learned: held-out room scenes")
+    p.add_argument("--eval-patches", type=int, default=50000, help="learned: patch target of a held-out room")
+    p.add_argument("--learned-w", type=int, default=128, help="learned: hemicube side of training and evaluation")
+    p.add_argument("--gen-workers", type=int, default=8, help="learned: scene-generation processes")
     return p.parse_args()
 
 
@@ -437,17 +445,22 @@ def run_precision(args):
     print(json.dumps(line), flush=True)
 
 
-def train_warm_start(args, scenes_n: int = 48, epochs: int = 200):
-    """Solver-generated training set (Cornell variants, 2k-6k patches, W=128) and the trained MLP."""
+def train_warm_start(args, scenes_n: int = 48, epochs: int = 200, patches=(2000, 6000), kinds=("cornell",),
+                     sample=None, W: int = 128, workers: int = 0):
+    """Solver-generated training set (seeded scenes, W=128 by default) and the trained MLP."""
     import radiosity_gb300 as R
     from radiosity_gb300 import learned
 
     t0 = time.perf_counter()
-    X, T = learned.training_set(scenes_n, seed=args.seed, patches=(2000, 6000), W=128)
+    X, T = learned.training_set(scenes_n, seed=args.seed, patches=patches, W=W, kinds=kinds, sample=sample,
+                                workers=workers)
     gen_s = time.perf_counter() - t0
+    order = np.random.default_rng(args.seed).permutation(X.shape[0])  # batches mix scenes
+    X, T = np.ascontiguousarray(X[order]), np.ascontiguousarray(T[order])
     m = R.MLP(seed=args.seed)
     loss, train_ms = m.train(X, T, epochs=epochs, batch=4096, lr=2e-3)
-    return m, {"scenes": scenes_n, "patches": int(X.shape[0]), "epochs": epochs, "final_loss": loss,
+    return m, {"scenes": scenes_n, "kinds": list(kinds), "patch_range": list(patches), "W": W,
+               "samples": int(X.shape[0]), "sample_per_scene": sample, "epochs": epochs, "final_loss": loss,
                "train_ms": train_ms, "data_gen_s": gen_s}
 
 
@@ -464,37 +477,61 @@ def learned_headline(args):
 
 
 def run_learned(args):
-    """Learned warm start: train the MLP on solver-generated Cornell-variant scenes, evaluate as the
-    gather's initial guess on held-out Cornell variants; iterations and time to 1e-4 per start."""
-    from radiosity_gb300 import learned, scenes
+    """Learned warm start: train the MLP on solver-generated scenes (rooms and Cornell variants,
+    patch counts log-uniform in --train-patches), then, on --eval-scenes held-out seeded rooms
+    of the large configuration's generator (40 boxes, 4 ceiling emitters, --eval-patches
+    patches), solve to 1e-4 with rad_gather_solve from three starts: emission, emission + direct
+    light, and the network's guess.  Reports refinements and device solve time per start."""
+    from radiosity_gb300 import learned
 
-    m, training = train_warm_start(args)
-    rows = []
-    for k in range(8):
-        sc = scenes.cornell_variant(6000, seed=10_000 + k)
-        with learned.capture(sc, W=128) as s:
+    lo, hi = (int(v) for v in args.train_patches.split(","))
+    W = args.learned_w
+    m, training = train_warm_start(args, scenes_n=args.train_scenes, epochs=args.train_epochs, patches=(lo, hi),
+                                   kinds=("room", "cornell"), sample=args.train_sample, W=W,
+                                   workers=args.gen_workers)
+    names = ("emission", "direct", "learned")
+    rows, caps, npat = [], [], []
+    t0 = time.perf_counter()
+    specs = [("room", args.eval_patches, 10_000 + k, 40, 4) for k in range(args.eval_scenes)]
+    for sc in learned.generated(specs, args.gen_workers):
+        c0 = time.perf_counter()
+        with learned.capture(sc, W=W) as s:
+            caps.append(time.perf_counter() - c0)
+            npat.append(sc["n"])
             E = learned.emission_block(sc)
             d = learned.direct_light(s, E)
             direct = np.ascontiguousarray((sc["radiosity"].reshape(-1, 3) + d).T, np.float32)
             guess = learned.warm_start(m, sc, d)
             res = {}
-            for name, g in (("emission", None), ("direct", direct), ("learned", guess)):
+            for name, g in zip(names, (None, direct, guess)):
                 _, st = s.gather(E, guess=g, tol=1e-4, max_outer=200, sweeps=4)
-                res[name] = (st.outer, st.sweeps, st.device_ms, st.initial_residual)
+                res[name] = (st.outer, st.sweeps, st.device_ms, st.initial_residual, st.residual)
             rows.append(res)
-    summ = {k: {"outer_mean": float(np.mean([r[k][0] for r in rows])),
-                "sweeps_mean": float(np.mean([r[k][1] for r in rows])),
-                "solve_ms_mean": float(np.mean([r[k][2] for r in rows])),
-                "initial_residual_mean": float(np.mean([r[k][3] for r in rows]))} for k in rows[0]}
+    eval_s = time.perf_counter() - t0
+    m.close()
+
+    def col(k, i):
+        return np.array([r[k][i] for r in rows], np.float64)
+
+    summ = {k: {"outer_mean": float(col(k, 0).mean()), "sweeps_mean": float(col(k, 1).mean()),
+                "solve_ms_mean": float(col(k, 2).mean()), "solve_ms_p50": float(np.percentile(col(k, 2), 50)),
+                "solve_ms_p99": float(np.percentile(col(k, 2), 99)),
+                "initial_residual_mean": float(col(k, 3).mean()), "final_residual_max": float(col(k, 4).max())}
+            for k in names}
     line = {"metric": "gather time-to-residual<=1e-4 from the learned guess", "value": summ["learned"]["solve_ms_mean"],
             "unit": "ms", "workload": "learned", "higher_is_better": False, "starts": summ,
+            "learned_faster_than_direct_fraction": float(np.mean(col("learned", 2) < col("direct", 2))),
+            "speedup_vs_emission": summ["emission"]["solve_ms_mean"] / summ["learned"]["solve_ms_mean"],
+            "speedup_vs_direct": summ["direct"]["solve_ms_mean"] / summ["learned"]["solve_ms_mean"],
             "training": training,
-            "config": {"workload": "MLP 32-128x4-3 BF16; trained on 48 Cornell-variant scenes (2k-6k patches, W=128); "
-                                   "evaluated on 8 held-out Cornell-variant scenes (6k patches, W=128)"},
+            "evaluation": {"scenes": len(rows), "patches_mean": float(np.mean(npat)), "W": W,
+                           "capture_s_mean": float(np.mean(caps)), "wall_s": eval_s},
+            "config": {"workload": f"MLP 32-128x4-3 BF16; trained on {args.train_scenes} solver-generated scenes "
+                                   f"(rooms and Cornell variants, {lo}-{hi} patches, W={W}, {args.train_sample} "
+                                   f"patches sampled per scene); evaluated on {args.eval_scenes} held-out seeded "
+                                   f"rooms (20x20x5 m, 40 boxes, 4 ceiling emitters, {args.eval_patches} patches, "
+                                   f"W={W})"},
             "data": "synthetic"}
-    if args.headline_patches:
-        line["headline"] = headline(args, m)
-    m.close()
     print(json.dumps(line), flush=True)
 
 

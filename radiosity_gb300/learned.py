@@ -22,6 +22,7 @@ _FOURIER = np.random.default_rng(1234).normal(0.0, 2.0, (8, 3)).astype(np.float6
 
 
 def patch_geometry(vertices: np.ndarray):
+    """Centres, unit normals and areas of the quads (N x 3, N x 3, N)."""
     q = vertices.reshape(-1, 4, 3).astype(np.float64)
     c = q.mean(1)
     n = np.cross(q[:, 3] - q[:, 0], q[:, 1] - q[:, 0])
@@ -36,8 +37,9 @@ def scale_of(direct: np.ndarray) -> np.ndarray:
 
 
 def features(scene: dict, direct: np.ndarray) -> np.ndarray:
-    """32 features per patch; direct is N x 3."""
-    c, n, a = patch_geometry(scene["vertices"])
+    """32 features per patch; direct is N x 3.  Uses scene["geometry"] (patch_geometry's
+    output) when a scene generator attached it."""
+    c, n, a = scene["geometry"] if "geometry" in scene else patch_geometry(scene["vertices"])
     lo, hi = c.min(0), c.max(0)
     p = (c - lo) / np.maximum(hi - lo, 1e-9)
     s = scale_of(direct)
@@ -79,19 +81,78 @@ def direct_light(solver: "_lib.Solver", E: np.ndarray) -> np.ndarray:
     return solver.gather_residual(E, E).T.astype(np.float64)
 
 
-def training_set(n_scenes: int, seed: int = 0, patches=(2000, 6000), W: int = 128, tol: float = 1e-6):
-    """Solver-generated (X, T) pairs from ``cornell_variant`` scenes."""
+def scene_specs(n_scenes: int, seed: int = 0, patches=(2000, 6000), kinds=("cornell",)) -> list:
+    """Seeded scene descriptions for training: the patch target is log-uniform in `patches`,
+    the kinds alternate.  A room varies its box count (10-60) and ceiling emitters (1-6); a
+    Cornell variant has one light when it is the only kind, else 1-3 lights in turn."""
     rng = np.random.default_rng(seed)
-    Xs, Ts = [], []
+    specs = []
     for k in range(n_scenes):
         target = int(np.exp(rng.uniform(np.log(patches[0]), np.log(patches[1]))))
-        sc = scenes.cornell_variant(target, seed=int(rng.integers(1 << 30)))
+        kind = kinds[k % len(kinds)]
+        s = int(rng.integers(1 << 30))
+        if kind == "room":
+            specs.append(("room", target, s, int(rng.integers(10, 61)), int(rng.integers(1, 7))))
+        else:
+            specs.append(("cornell", target, s, 1 if len(kinds) == 1 else 1 + (k // len(kinds)) % 3, 0))
+    return specs
+
+
+def make_scene(spec) -> dict:
+    """The scene of one scene_specs entry, with its patch geometry attached (runs in worker
+    processes too: it touches no device)."""
+    kind, target, seed, a, b = spec
+    if kind == "room":
+        sc = scenes.room_with_boxes(target=target, seed=seed, n_boxes=a, n_emitters=b)
+    else:
+        sc = scenes.cornell_variant(target, seed=seed, n_lights=a)
+    sc["geometry"] = patch_geometry(sc["vertices"])
+    return sc
+
+
+def generated(specs, workers: int = 0):
+    """Yields make_scene(spec) in order.  With workers > 0 the scenes are made ahead in a
+    spawn-started process pool (at most 2 * workers in flight), so host generation overlaps
+    the caller's device work."""
+    if workers <= 0:
+        for sp in specs:
+            yield make_scene(sp)
+        return
+    import collections
+    import multiprocessing
+
+    with multiprocessing.get_context("spawn").Pool(workers) as pool:
+        pending = collections.deque()
+        it = iter(specs)
+        for sp in it:
+            pending.append(pool.apply_async(make_scene, (sp,)))
+            if len(pending) >= 2 * workers:
+                break
+        while pending:
+            sc = pending.popleft().get()
+            for sp in it:
+                pending.append(pool.apply_async(make_scene, (sp,)))
+                break
+            yield sc
+
+
+def training_set(n_scenes: int, seed: int = 0, patches=(2000, 6000), W: int = 128, tol: float = 1e-6,
+                 kinds=("cornell",), sample: int | None = None, workers: int = 0):
+    """Solver-generated (X, T) pairs: each scene of scene_specs is captured at hemicube side W
+    and solved by rad_gather_solve to `tol`; `sample` keeps at most that many random patches
+    per scene (a seeded choice)."""
+    Xs, Ts = [], []
+    for k, sc in enumerate(generated(scene_specs(n_scenes, seed, patches, kinds), workers)):
         with capture(sc, W) as s:
             E = emission_block(sc)
             B, _ = s.gather(E, tol=tol, max_outer=80, sweeps=8)
             d = direct_light(s, E)
-        Xs.append(features(sc, d))
-        Ts.append(targets(sc, B.T.astype(np.float64), d))
+        X, T = features(sc, d), targets(sc, B.T.astype(np.float64), d)
+        if sample is not None and sc["n"] > sample:
+            idx = np.random.default_rng((seed, k)).choice(sc["n"], sample, replace=False)
+            X, T = X[idx], T[idx]
+        Xs.append(X)
+        Ts.append(T)
     return np.concatenate(Xs), np.concatenate(Ts)
 
 
