@@ -505,7 +505,8 @@ def run_learned(args):
             res = {}
             for name, g in zip(names, (None, direct, guess)):
                 _, st = s.gather(E, guess=g, tol=1e-4, max_outer=200, sweeps=4)
-                res[name] = (st.outer, st.sweeps, st.device_ms, st.initial_residual, st.residual)
+                res[name] = (st.outer, st.sweeps, st.device_ms, st.initial_residual, st.residual, st.sweep_ms,
+                             st.resid_ms)
             rows.append(res)
     eval_s = time.perf_counter() - t0
     m.close()
@@ -516,7 +517,8 @@ def run_learned(args):
     summ = {k: {"outer_mean": float(col(k, 0).mean()), "sweeps_mean": float(col(k, 1).mean()),
                 "solve_ms_mean": float(col(k, 2).mean()), "solve_ms_p50": float(np.percentile(col(k, 2), 50)),
                 "solve_ms_p99": float(np.percentile(col(k, 2), 99)),
-                "initial_residual_mean": float(col(k, 3).mean()), "final_residual_max": float(col(k, 4).max())}
+                "initial_residual_mean": float(col(k, 3).mean()), "final_residual_max": float(col(k, 4).max()),
+                "sweep_ms_mean": float(col(k, 5).mean()), "resid_ms_mean": float(col(k, 6).mean())}
             for k in names}
     line = {"metric": "gather time-to-residual<=1e-4 from the learned guess", "value": summ["learned"]["solve_ms_mean"],
             "unit": "ms", "workload": "learned", "higher_is_better": False, "starts": summ,
@@ -686,7 +688,7 @@ def uneven_gather(args, scs, tol, tune, checks: int = 4, workers: int = 4):
     """The uneven batch by learned warm start + BF16 gather: `workers` host threads take the
     scenes in turn, each with its own context (its own CUDA stream), so one scene's host work
     (upload, features) overlaps other scenes' GPU work.  The shared network is used under a
-    lock.  FP64 residuals of the first `checks` scenes are computed on the host afterwards."""
+    lock.  FP64 residuals of the first `checks` scenes are computed on the host after the pool."""
     import threading
     from concurrent.futures import ThreadPoolExecutor
 
@@ -710,18 +712,22 @@ def uneven_gather(args, scs, tol, tune, checks: int = 4, workers: int = 4):
                 guess = learned.warm_start(m, sc, direct)
             B, st = s.gather(E, guess=guess, tol=tol, max_outer=100, sweeps=4)
             wall = time.perf_counter() - t0
-            check = None
-            if k < checks:  # FP64 residual of the gather system on the FP32 rows
-                n = sc["n"]
-                F, _, _ = s.dense_rows(0, n)
-                rho = sc["reflectance"].reshape(n, 3).astype(np.float64)
-                E64 = E.T.astype(np.float64)
-                Bd = B.T.astype(np.float64)
-                r = E64 + rho * (F.astype(np.float64) @ Bd) - Bd
-                check = float(np.max(np.linalg.norm(r, axis=0) / np.maximum(np.linalg.norm(E64, axis=0), 1e-30)))
-            return wall, cap_ms / 1000 + st.device_ms / 1000, st.outer, check
+            # the FP32 rows of checked scenes are kept for the FP64 check after the pool (host
+            # BLAS is not called from several threads at once)
+            keep = (s.dense_rows(0, sc["n"])[0], E, B) if k < checks else None
+            return wall, cap_ms / 1000 + st.device_ms / 1000, st.outer, keep
         finally:
             s.close()
+
+    def fp64_check(k, keep):
+        """FP64 residual of the gather system on the FP32 rows."""
+        F, E, B = keep
+        n = scs[k]["n"]
+        rho = scs[k]["reflectance"].reshape(n, 3).astype(np.float64)
+        E64 = E.T.astype(np.float64)
+        Bd = B.T.astype(np.float64)
+        r = E64 + rho * (F.astype(np.float64) @ Bd) - Bd
+        return float(np.max(np.linalg.norm(r, axis=0) / np.maximum(np.linalg.norm(E64, axis=0), 1e-30)))
 
     t_all = time.perf_counter()
     try:
@@ -733,12 +739,12 @@ def uneven_gather(args, scs, tol, tune, checks: int = 4, workers: int = 4):
     wall = [r[0] for r in res]
     dev = [r[1] for r in res]
     outer = [r[2] for r in res]
-    fp64 = [r[3] for r in res if r[3] is not None]
+    fp64 = [fp64_check(k, r[3]) for k, r in enumerate(res) if r[3] is not None]
     return {"scenes_per_s": len(scs) / total, "wall_s": total, "host_threads": workers,
             "per_scene_s": {"p50": float(np.percentile(wall, 50)), "p99": float(np.percentile(wall, 99))},
             "per_scene_device_s": {"p50": float(np.percentile(dev, 50)), "p99": float(np.percentile(dev, 99))},
             "refinements_mean": float(np.mean(outer)), "hemicubes": int(sum(sc["n"] for sc in scs)),
-            "fp64_residual_max_checked": max(fp64) if fp64 else None, "fp64_checked_scenes": len(fp64),
+            "fp64_residual_max_checked": float(np.max(fp64)) if fp64 else None, "fp64_checked_scenes": len(fp64),
             "tol": tol, "training": training,
             "note": f"{workers} host threads, one context (stream) per scene in flight; per-scene times run from "
                     "the scene's start (upload) to its solution, the FP64 check excluded; the plain shooter's "

@@ -23,6 +23,7 @@ extern "C" {
 #define RAD_E_NOMEM (-5)    /* device allocation failed */
 #define RAD_E_TIMEOUT (-6)  /* a bounded device wait gave up */
 #define RAD_E_NOALLOC_LIMIT (-7) /* request larger than the allocation-free entry point's fixed scratch */
+#define RAD_E_NUMERIC (-8)  /* an iterative solve met a non-finite residual (NaN / inf in its data) */
 
 typedef enum { RAD_MODE_REF = 0, RAD_MODE_PHYS = 1 } rad_mode;
 
@@ -173,7 +174,9 @@ typedef struct rad_gather_stats {
 /* Solves B = E + rho o (F B) for R <= 256 right-hand sides, column-major N x R host
  * arrays (column c uses reflectance channel c % 3).  guess may be NULL (start from E).
  * Stops when the relative residual <= tol or after max_outer refinements; each
- * refinement runs `sweeps` BF16 sweeps.  Needs rad_dense_capture(RAD_DENSE_FP32). */
+ * refinement runs `sweeps` BF16 sweeps.  Needs rad_dense_capture(RAD_DENSE_FP32).
+ * RAD_E_INVALID when emission or guess holds NaN / inf; RAD_E_NUMERIC when a residual norm
+ * is not finite (radiosity then holds the last iterate). */
 int rad_gather_solve(rad_ctx* ctx, const float* emission, uint32_t R, const float* guess, double tol,
                      uint32_t max_outer, uint32_t sweeps, float* radiosity, rad_gather_stats* stats);
 

@@ -24,6 +24,7 @@ RAD_E_STATE = -4
 RAD_E_NOMEM = -5
 RAD_E_TIMEOUT = -6
 RAD_E_NOALLOC_LIMIT = -7
+RAD_E_NUMERIC = -8
 NOALLOC_MAX_SUMS = 1 << 20
 MODE_REF, MODE_PHYS = 0, 1
 

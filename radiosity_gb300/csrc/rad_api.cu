@@ -893,7 +893,7 @@ int rad_gather_solve(rad_ctx* c, const float* emission, uint32_t R, const float*
     const uint32_t n = c->n, ld = c->dense_ld;
     const size_t nr = (size_t)n * R;
     cudaStream_t s = c->stream;
-    float *dE = nullptr, *dB = nullptr, *dr = nullptr, *dd = nullptr, *dpart = nullptr;
+    float *dE = nullptr, *dB = nullptr, *dr = nullptr, *dd = nullptr, *dpart = nullptr, *dxp = nullptr;
     __nv_bfloat16* d16[2] = {nullptr, nullptr};
     const uint32_t ksplit = gemm_tc_ksplit(n, ld, Rpad);
     double* dnrm = nullptr;
@@ -901,7 +901,7 @@ int rad_gather_solve(rad_ctx* c, const float* emission, uint32_t R, const float*
     int rc = RAD_OK;
     auto cleanup = [&]() {
         cudaFree(dE); cudaFree(dB); cudaFree(dr); cudaFree(dd);
-        cudaFree(d16[0]); cudaFree(d16[1]); cudaFree(dnrm); cudaFree(derr); cudaFree(dpart);
+        cudaFree(d16[0]); cudaFree(d16[1]); cudaFree(dnrm); cudaFree(derr); cudaFree(dpart); cudaFree(dxp);
     };
 #define G_CUDA(call)                                                                                  \
     do {                                                                                              \
@@ -918,7 +918,14 @@ int rad_gather_solve(rad_ctx* c, const float* emission, uint32_t R, const float*
     G_CUDA(cudaMalloc(&dd, 4 * nr));
     G_CUDA(cudaMalloc(&d16[0], 2 * (size_t)Rpad * ld));
     G_CUDA(cudaMalloc(&d16[1], 2 * (size_t)Rpad * ld));
+    // The sweeps' epilogue writes only columns c < R and rows i < n of its BF16 output, and
+    // the next sweep multiplies the whole padded operand by F's zero padding: the padding
+    // must hold zeros, not leftover bits (0 x NaN = NaN).  k_pack_bf16 rewrites d16[0] in
+    // full; d16[1] is cleared once here.
+    G_CUDA(cudaMemsetAsync(d16[0], 0, 2 * (size_t)Rpad * ld, s));
+    G_CUDA(cudaMemsetAsync(d16[1], 0, 2 * (size_t)Rpad * ld, s));
     G_CUDA(cudaMalloc(&dnrm, 8 * (size_t)R));
+    if (const size_t xs = sgemm_resid_scratch_floats(R, ld)) G_CUDA(cudaMalloc(&dxp, 4 * xs));
     if (ksplit > 1) G_CUDA(cudaMalloc(&dpart, 4 * nr * ksplit));
     G_CUDA(cudaMalloc(&derr, 4));
     G_CUDA(cudaMemsetAsync(derr, 0, 4, s));
@@ -930,6 +937,13 @@ int rad_gather_solve(rad_ctx* c, const float* emission, uint32_t R, const float*
         for (uint32_t i = 0; i < n; i++) a += (double)emission[(size_t)col * n + i] * emission[(size_t)col * n + i];
         enorm[col] = std::sqrt(a);
     }
+    bool finite = true;
+    for (uint32_t col = 0; col < R; col++) finite = finite && std::isfinite(enorm[col]);
+    for (size_t i = 0; guess && finite && i < nr; i++) finite = std::isfinite(guess[i]);
+    if (!finite) {
+        cleanup();
+        return fail(c, RAD_E_INVALID, "emission or guess holds NaN / inf");
+    }
     cudaEvent_t ev[4];
     for (auto& e : ev) G_CUDA(cudaEventCreate(&e));
     G_CUDA(cudaEventRecord(ev[0], s));
@@ -938,7 +952,7 @@ int rad_gather_solve(rad_ctx* c, const float* emission, uint32_t R, const float*
     for (uint32_t outer = 0;; outer++) {
         G_CUDA(cudaMemsetAsync(dnrm, 0, 8 * (size_t)R, s));
         G_CUDA(cudaEventRecord(ev[2], s));
-        launch_sgemm_resid(c->d_F32, n, ld, dB, dE, c->d_rho, R, dr, dnrm, s);
+        launch_sgemm_resid(c->d_F32, n, ld, dB, dE, c->d_rho, R, dr, dnrm, dxp, derr, s);
         G_CUDA(cudaEventRecord(ev[3], s));
         G_CUDA(cudaGetLastError());
         G_CUDA(cudaMemcpyAsync(nrm.data(), dnrm, 8 * (size_t)R, cudaMemcpyDeviceToHost, s));
@@ -947,11 +961,18 @@ int rad_gather_solve(rad_ctx* c, const float* emission, uint32_t R, const float*
         cudaEventElapsedTime(&ms, ev[2], ev[3]);
         resid_ms += ms;
         double res = 0;
-        for (uint32_t col = 0; col < R; col++)
+        bool bad = false;
+        for (uint32_t col = 0; col < R; col++) {
+            bad = bad || !std::isfinite(nrm[col]);
             if (enorm[col] > 0) res = std::max(res, std::sqrt(nrm[col]) / enorm[col]);
+        }
         st.outer = outer + 1;
-        if (outer == 0) st.initial_residual = res;
-        st.residual = res;
+        if (outer == 0) st.initial_residual = bad ? NAN : res;
+        st.residual = bad ? NAN : res;
+        if (bad) {  // NaN would compare as converged
+            rc = fail(c, RAD_E_NUMERIC, "a residual norm is not finite");
+            break;
+        }
         if (res <= tol || outer >= max_outer) break;
         // correction: d = r + rho o (F16 d), d0 = r
         if (sweeps == 0) {
@@ -1004,7 +1025,7 @@ int rad_gather_solve(rad_ctx* c, const float* emission, uint32_t R, const float*
     st.sweep_ms = sweep_ms;
     st.resid_ms = resid_ms;
     if (stats) *stats = st;
-    if (herr) rc = fail(c, RAD_E_TIMEOUT, "a tcgen05 pipeline wait timed out");
+    if (herr) rc = fail(c, RAD_E_TIMEOUT, "a tcgen05 or residual pipeline wait timed out");
     return rc;
 }
 
@@ -1012,22 +1033,32 @@ int rad_gather_residual(rad_ctx* c, const float* emission, uint32_t R, const flo
     if (!c || !emission || !radiosity || !residual || R == 0) return RAD_E_INVALID;
     if (!c->dense_ready || !c->d_F32) return fail(c, RAD_E_STATE, "needs rad_dense_capture with RAD_DENSE_FP32");
     const size_t nr = (size_t)c->n * R;
-    float *dE = nullptr, *dB = nullptr, *dr = nullptr;
+    float *dE = nullptr, *dB = nullptr, *dr = nullptr, *dxp = nullptr;
+    uint32_t* derr = nullptr;
+    uint32_t herr = 0;
     int rc = RAD_OK;
+    const size_t xs = sgemm_resid_scratch_floats(R, c->dense_ld);
     if (cudaMalloc(&dE, 4 * nr) != cudaSuccess || cudaMalloc(&dB, 4 * nr) != cudaSuccess ||
-        cudaMalloc(&dr, 4 * nr) != cudaSuccess)
+        cudaMalloc(&dr, 4 * nr) != cudaSuccess || cudaMalloc(&derr, 4) != cudaSuccess ||
+        (xs && cudaMalloc(&dxp, 4 * xs) != cudaSuccess))
         rc = fail(c, RAD_E_NOMEM, "residual buffers");
     if (!rc) {
+        cudaMemsetAsync(derr, 0, 4, c->stream);
         cudaMemcpyAsync(dE, emission, 4 * nr, cudaMemcpyHostToDevice, c->stream);
         cudaMemcpyAsync(dB, radiosity, 4 * nr, cudaMemcpyHostToDevice, c->stream);
-        launch_sgemm_resid(c->d_F32, c->n, c->dense_ld, dB, dE, c->d_rho, R, dr, nullptr, c->stream);
+        launch_sgemm_resid(c->d_F32, c->n, c->dense_ld, dB, dE, c->d_rho, R, dr, nullptr, dxp, derr, c->stream);
         cudaMemcpyAsync(residual, dr, 4 * nr, cudaMemcpyDeviceToHost, c->stream);
+        cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, c->stream);
         if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(c->stream) != cudaSuccess)
             rc = fail(c, RAD_E_CUDA, "residual GEMM failed");
+        else if (herr)
+            rc = fail(c, RAD_E_TIMEOUT, "a residual pipeline wait timed out");
     }
     cudaFree(dE);
     cudaFree(dB);
     cudaFree(dr);
+    cudaFree(dxp);
+    cudaFree(derr);
     return rc;
 }
 
@@ -1306,6 +1337,7 @@ const char* rad_strerror(int status) {
         case RAD_E_NOMEM: return "device allocation failed";
         case RAD_E_TIMEOUT: return "bounded device wait gave up";
         case RAD_E_NOALLOC_LIMIT: return "count * n_patches exceeds RAD_NOALLOC_MAX_SUMS (allocation-free scratch)";
+        case RAD_E_NUMERIC: return "non-finite residual";
         default: return "unknown status";
     }
 }

@@ -158,8 +158,12 @@ struct TcEpilogue {
 };
 void launch_dense_rows(unsigned long long* Fq, uint32_t count, uint32_t n, uint32_t ld, uint32_t first,
                        float* F32, __nv_bfloat16* F16, float* scale, cudaStream_t s);
+// r = E + rho o (F X) - X; R <= 4 takes the streaming kernel, which needs `scratch` of
+// sgemm_resid_scratch_floats(R, ld) floats (0 for larger R: scratch may be null) and sets
+// *err (when given) if one of its bounded pipeline waits timed out.
+size_t sgemm_resid_scratch_floats(uint32_t R, uint32_t ld);
 void launch_sgemm_resid(const float* F, uint32_t n, uint32_t ld, const float* X, const float* E, const float4* rho,
-                        uint32_t R, float* r, double* nrm, cudaStream_t s);
+                        uint32_t R, float* r, double* nrm, float* scratch, uint32_t* err, cudaStream_t s);
 void launch_shoot_resid(const float* F, uint32_t n, uint32_t ld, const float* X, const float* E, const float4* rho,
                         const float* area, uint32_t R, double* acc, float* r, cudaStream_t s);
 void launch_pack_bf16(const float* X, uint32_t n, uint32_t R, uint32_t ld, __nv_bfloat16* Xt, uint32_t Rpad,

@@ -58,8 +58,11 @@ def targets(scene: dict, B: np.ndarray, direct: np.ndarray) -> np.ndarray:
 
 
 def decode(scene: dict, direct: np.ndarray, Y: np.ndarray) -> np.ndarray:
+    """B0 = E + s * expm1(y), y clipped to [0, 30] (a non-finite output counts as 0, i.e. the
+    emission alone), so the guess is always finite."""
     E = scene["radiosity"].reshape(-1, 3).astype(np.float64)
-    return (E + scale_of(direct) * np.expm1(np.maximum(Y, 0))).astype(np.float32)
+    y = np.where(np.isfinite(Y), np.clip(Y, 0.0, 30.0), 0.0)
+    return (E + scale_of(direct) * np.expm1(y)).astype(np.float32)
 
 
 def capture(scene: dict, W: int = 128) -> "_lib.Solver":

@@ -61,11 +61,33 @@ def test_dense_capture_rows(lib, box):
     assert np.all(np.abs(approx - f32) <= 2.0 ** -8 * scale[:, None] + 1e-30)
 
 
-def test_gather_solve_matches_fp64(lib, box):
+@pytest.mark.parametrize("R", [1, 3, 4, 5, 6, 70])
+def test_gather_residual_matches_fp64(lib, box, R):
+    """r = E + rho o (F B) - B: the narrow kernel (R <= 4) and the tiled one (R > 4) against
+    an FP64 evaluation on the same FP32 rows, elementwise within 1e-6 of the terms' size."""
+    n = box["n"]
+    rng = np.random.default_rng(100 + R)
+    E = rng.uniform(0, 5, (R, n)).astype(np.float32)
+    B = rng.uniform(0, 10, (R, n)).astype(np.float32)
+    with _solver(lib, box) as s:
+        s.dense_capture(keep_fp32=True)
+        F, _, _ = s.dense_rows(0, n)
+        r = s.gather_residual(E, B)
+    rho = box["reflectance"].reshape(n, 3).astype(np.float64)
+    F64 = F.astype(np.float64)
+    for c in range(R):
+        rc = rho[:, c % 3]
+        ref = E[c] + rc * (F64 @ B[c].astype(np.float64)) - B[c]
+        size = np.abs(E[c]) + rc * (np.abs(F64) @ np.abs(B[c].astype(np.float64))) + np.abs(B[c])
+        assert np.all(np.abs(r[c] - ref) <= 1e-6 * size), c
+
+
+@pytest.mark.parametrize("emitters", [1, 2])
+def test_gather_solve_matches_fp64(lib, box, emitters):
     n = box["n"]
     rng = np.random.default_rng(3)
-    E = np.zeros((6, n), np.float32)
-    for v in range(2):  # two emission vectors x RGB
+    E = np.zeros((3 * emitters, n), np.float32)
+    for v in range(emitters):  # emission vectors x RGB
         em = rng.choice(n, 3, replace=False)
         E[3 * v:3 * v + 3, em] = rng.uniform(1, 20, (3, 3)).astype(np.float32)
     with _solver(lib, box) as s:
@@ -75,7 +97,7 @@ def test_gather_solve_matches_fp64(lib, box):
     assert st.residual <= 1e-6 and st.sweeps > 0
     rho = box["reflectance"].reshape(n, 3).astype(np.float64)
     F64 = F.astype(np.float64)
-    for c in range(6):
+    for c in range(3 * emitters):
         A = np.eye(n) - rho[:, c % 3][:, None] * F64
         ref = np.linalg.solve(A, E[c].astype(np.float64))
         assert np.linalg.norm(B[c] - ref) <= 1e-5 * np.linalg.norm(ref)
@@ -114,3 +136,44 @@ def test_shoot_residual_matches_fp64_and_the_shooter_converges_on_it(lib, box):
             Bt = (rad.astype(np.float64) + ill).reshape(n, 3).T.astype(np.float32)
             res.append(np.linalg.norm(s.shoot_residual(E, Bt).astype(np.float64)) / np.linalg.norm(E))
         assert res[1] < 0.1 * res[0] and res[1] < 1e-3
+
+
+def test_gather_rejects_non_finite_inputs(lib, box):
+    """A NaN guess or emission is refused before any device work; NaN must never pass the
+    convergence test (NaN <= tol is false, but a max() over NaN would hide it)."""
+    n = box["n"]
+    E = np.zeros((3, n), np.float32)
+    E[:, 0] = 5.0
+    with _solver(lib, box) as s:
+        s.dense_capture(keep_fp32=True)
+        g = np.array(E, copy=True)
+        g[1, n // 2] = np.nan
+        with pytest.raises(lib.RadError) as e:
+            s.gather(E, guess=g, tol=1e-6)
+        assert e.value.status == lib._lib.RAD_E_INVALID
+        bad = np.array(E, copy=True)
+        bad[2, 3] = np.inf
+        with pytest.raises(lib.RadError) as e:
+            s.gather(bad, tol=1e-6)
+        assert e.value.status == lib._lib.RAD_E_INVALID
+        B, st = s.gather(E, tol=1e-6, max_outer=60, sweeps=6)  # the context stays usable
+        assert st.residual <= 1e-6 and np.all(np.isfinite(B))
+
+
+def test_gather_ignores_leftover_device_memory(lib, box):
+    """The solve's device buffers come from cudaMalloc and may hold a previous owner's bits.
+    Memory filled with NaN and handed back to the driver must not leak into the result (the
+    BF16 operands' row padding is multiplied by F's zero padding, and 0 x NaN = NaN)."""
+    torch = pytest.importorskip("torch")
+    n = box["n"]
+    E = np.zeros((3, n), np.float32)
+    E[:, [0, n // 3]] = 7.0
+    with _solver(lib, box) as s:
+        s.dense_capture(keep_fp32=True)
+        for _ in range(3):
+            junk = torch.full((64 << 20,), float("nan"), dtype=torch.float32, device="cuda:0")
+            torch.cuda.synchronize()
+            del junk
+            torch.cuda.empty_cache()
+            B, st = s.gather(E, tol=1e-6, max_outer=60, sweeps=6)
+            assert st.residual <= 1e-6 and np.all(np.isfinite(B))
