@@ -373,9 +373,17 @@ class Solver:
         i = None if illumination is None else np.ascontiguousarray(illumination, np.float32).reshape(-1)
         self._check(self.L.rad_set_state(self.h, _ptr(r), _ptr(i)), "rad_set_state")
 
-    def download(self):
-        r = np.zeros(3 * self.n, np.float32)
-        i = np.zeros(3 * self.n, np.float32)
+    def download(self, out=None):
+        """rad_download: (radiosity, illumination) as N x 3 float32 arrays, written into
+        `out` = (r, i) when given (contiguous float32 arrays of 3N, e.g. pinned buffers)."""
+        if out is None:
+            r = np.empty(3 * self.n, np.float32)
+            i = np.empty(3 * self.n, np.float32)
+        else:
+            r, i = out
+            for a in (r, i):
+                if a.dtype != np.float32 or a.size != 3 * self.n or not a.flags.c_contiguous:
+                    raise ValueError("download(out=...) needs two contiguous float32 arrays of 3N")
         self._check(self.L.rad_download(self.h, _ptr(r), _ptr(i)), "rad_download")
         return r, i
 

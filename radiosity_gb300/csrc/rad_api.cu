@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <unistd.h>
 #include <string>
 #include <vector>
 
@@ -57,7 +58,7 @@ struct rad_ctx {
     DevState* d_state = nullptr;   // shoot loop state
     DevState* d_aux = nullptr;     // state for the one-off entry points
     uint32_t* h_flag = nullptr;    // pinned stop flag
-    float4* h_stage = nullptr;     // pinned staging for the state copies, 2 x N float4 (null: pageable path)
+    float* d_f3 = nullptr;         // device scratch for the host's float3 arrays, 2 x 3N floats
     BatchBuf shoot;                // K = hemicubes_count
     BatchBuf aux;                  // one-off calls, grown on demand
     float* d_rows = nullptr;       // float rows for ff_rows / reduce
@@ -397,7 +398,7 @@ int rad_destroy(rad_ctx* c) {
     dfree(c->d_F16);
     dfree(c->d_scale);
     if (c->h_flag) cudaFreeHost(c->h_flag);
-    if (c->h_stage) cudaFreeHost(c->h_stage);
+    dfree(c->d_f3);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -405,11 +406,19 @@ int rad_destroy(rad_ctx* c) {
     return RAD_OK;
 }
 
-static int upload_f3(rad_ctx* c, float4* dst, const float* src, uint32_t n) {
-    std::vector<float4> tmp(n);
-    for (uint32_t i = 0; i < n; i++)
-        tmp[i] = src ? make_float4(src[3 * i], src[3 * i + 1], src[3 * i + 2], 0.f) : make_float4(0, 0, 0, 0);
-    RAD_CUDA(c, cudaMemcpy(dst, tmp.data(), sizeof(float4) * n, cudaMemcpyHostToDevice));
+// Host float3 array (N x 3, any host memory) -> device float4 rows, on the context's stream:
+// one DMA of the caller's bytes into scratch slot `slot` of d_f3, widened on the device (no
+// host-side packing loop).  A null src zeroes the rows.  Ordered in the stream, so the next
+// use of the slot waits for this one.
+static int upload_f3(rad_ctx* c, float4* dst, const float* src, uint32_t n, int slot) {
+    if (!src) {
+        RAD_CUDA(c, cudaMemsetAsync(dst, 0, sizeof(float4) * n, c->stream));
+        return RAD_OK;
+    }
+    float* tmp = c->d_f3 + (size_t)slot * 3 * n;
+    RAD_CUDA(c, cudaMemcpyAsync(tmp, src, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    launch_f3_to_f4(tmp, dst, n, c->stream);
+    RAD_CUDA(c, cudaGetLastError());
     return RAD_OK;
 }
 
@@ -443,6 +452,7 @@ int rad_upload_scene(rad_ctx* c, const float* vertices, const int32_t* indices, 
     dfree(c->d_area);
     dfree(c->d_nb);
     dfree(c->d_shade);
+    dfree(c->d_f3);
     c->n = n;
     c->geo.n = n;
     RAD_CUDA(c, cudaMalloc(&c->d_verts, sizeof(float) * 12 * (size_t)n));
@@ -451,18 +461,14 @@ int rad_upload_scene(rad_ctx* c, const float* vertices, const int32_t* indices, 
     RAD_CUDA(c, cudaMalloc(&c->d_rad, sizeof(float4) * n));
     RAD_CUDA(c, cudaMalloc(&c->d_illum, sizeof(float4) * n));
     RAD_CUDA(c, cudaMalloc(&c->d_area, sizeof(float) * n));
-    RAD_CUDA(c, cudaMemcpy(c->d_verts, vertices, sizeof(float) * 12 * (size_t)n, cudaMemcpyHostToDevice));
+    RAD_CUDA(c, cudaMalloc(&c->d_f3, sizeof(float) * 6 * (size_t)n));
+    RAD_CUDA(c, cudaMemcpyAsync(c->d_verts, vertices, sizeof(float) * 12 * (size_t)n, cudaMemcpyHostToDevice,
+                                c->stream));
     int rc;
-    if ((rc = upload_f3(c, c->d_color, color, n))) return rc;
-    if ((rc = upload_f3(c, c->d_rho, reflectance, n))) return rc;
-    if ((rc = upload_f3(c, c->d_rad, radiosity, n))) return rc;
-    if ((rc = upload_f3(c, c->d_illum, illumination, n))) return rc;
-    if (c->h_stage) cudaFreeHost(c->h_stage);
-    c->h_stage = nullptr;
-    if (cudaMallocHost(&c->h_stage, sizeof(float4) * 2 * (size_t)n) != cudaSuccess) {
-        c->h_stage = nullptr;  // the state copies then go through pageable memory
-        cudaGetLastError();
-    }
+    if ((rc = upload_f3(c, c->d_color, color, n, 0))) return rc;
+    if ((rc = upload_f3(c, c->d_rho, reflectance, n, 1))) return rc;
+    if ((rc = upload_f3(c, c->d_rad, radiosity, n, 0))) return rc;
+    if ((rc = upload_f3(c, c->d_illum, illumination, n, 1))) return rc;
     launch_areas(c->d_verts, n, c->d_area, c->stream);
     RAD_CUDA(c, cudaMemsetAsync(c->d_state, 0, sizeof(DevState), c->stream));
     launch_power0(c->d_rad, c->d_area, n, c->d_state, c->stream);
@@ -476,48 +482,50 @@ int rad_set_state(rad_ctx* c, const float* radiosity, const float* illumination)
     if (!c) return RAD_E_INVALID;
     if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
     RAD_CUDA(c, cudaStreamSynchronize(c->stream));
-    const size_t n = c->n;
     int rc;
-    if (c->h_stage) {  // pack into pinned memory, two asynchronous copies, one wait
-        const float* src[2] = {radiosity, illumination};
-        float4* dst[2] = {c->d_rad, c->d_illum};
-        for (int k = 0; k < 2; k++) {
-            if (!src[k]) continue;
-            float4* st = c->h_stage + k * n;
-            for (size_t i = 0; i < n; i++) st[i] = make_float4(src[k][3 * i], src[k][3 * i + 1], src[k][3 * i + 2], 0.f);
-            RAD_CUDA(c, cudaMemcpyAsync(dst[k], st, sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream));
-        }
-    } else {
-        if (radiosity && (rc = upload_f3(c, c->d_rad, radiosity, c->n))) return rc;
-        if (illumination && (rc = upload_f3(c, c->d_illum, illumination, c->n))) return rc;
-    }
+    if (radiosity && (rc = upload_f3(c, c->d_rad, radiosity, c->n, 0))) return rc;
+    if (illumination && (rc = upload_f3(c, c->d_illum, illumination, c->n, 1))) return rc;
     RAD_CUDA(c, cudaMemsetAsync(&c->d_state->stopped, 0, sizeof(uint32_t), c->stream));
     RAD_CUDA(c, cudaStreamSynchronize(c->stream));
     return RAD_OK;
 }
 
+// Touches one byte per page of a pageable destination before a device-to-host copy into it.
+// Where the GPU reaches host memory through the host's page tables (NVLink-C2C systems), a
+// copy into never-touched pages faults each page in from the GPU side: measured on GB300,
+// 155 us for a 606 KB array of fresh 64 KB pages, against ~49 us when the CPU populates them
+// first.  Pinned or registered memory is left alone.  The bytes written are overwritten by
+// the copy.
+static void prefault_pageable(void* p, size_t bytes) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    if (a.type != cudaMemoryTypeUnregistered) return;
+    static const size_t page = (size_t)sysconf(_SC_PAGESIZE);
+    volatile char* b = static_cast<volatile char*>(p);
+    for (size_t o = 0; o < bytes; o += page) b[o] = 0;
+    if (bytes) b[bytes - 1] = 0;
+}
+
+// Device float4 rows -> the caller's float3 arrays: narrowed on the device into the scratch,
+// then one DMA per array straight into the caller's memory.
 int rad_download(rad_ctx* c, float* radiosity, float* illumination) {
     if (!c) return RAD_E_INVALID;
     if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
     const size_t n = c->n;
     float* dst[2] = {radiosity, illumination};
-    float4* src[2] = {c->d_rad, c->d_illum};
-    std::vector<float4> tmp;
-    if (!c->h_stage) tmp.resize(2 * n);
-    float4* stage = c->h_stage ? c->h_stage : tmp.data();
-    for (int k = 0; k < 2; k++)
-        if (dst[k])
-            RAD_CUDA(c, cudaMemcpyAsync(stage + k * n, src[k], sizeof(float4) * n, cudaMemcpyDeviceToHost, c->stream));
-    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    const float4* src[2] = {c->d_rad, c->d_illum};
     for (int k = 0; k < 2; k++) {
         if (!dst[k]) continue;
-        const float4* st = stage + k * n;
-        for (size_t i = 0; i < n; i++) {
-            dst[k][3 * i] = st[i].x;
-            dst[k][3 * i + 1] = st[i].y;
-            dst[k][3 * i + 2] = st[i].z;
-        }
+        float* tmp = c->d_f3 + (size_t)k * 3 * n;
+        prefault_pageable(dst[k], sizeof(float) * 3 * n);
+        launch_f4_to_f3(src[k], tmp, c->n, c->stream);
+        RAD_CUDA(c, cudaGetLastError());
+        RAD_CUDA(c, cudaMemcpyAsync(dst[k], tmp, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
     }
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
     return RAD_OK;
 }
 

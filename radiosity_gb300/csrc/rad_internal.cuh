@@ -133,6 +133,8 @@ void launch_update(const Geo& g, const Batch& b, const float4* color, const floa
 void launch_emitters(const Geo& g, const Batch& b, float4* rad, float4* illum, const float* area,
                      double tol, double* partials, DevState* st, cudaStream_t s);
 void launch_areas(const float* verts, uint32_t n, float* area, cudaStream_t s);
+void launch_f3_to_f4(const float* src, float4* dst, uint32_t n, cudaStream_t s);
+void launch_f4_to_f3(const float4* src, float* dst, uint32_t n, cudaStream_t s);
 // display.cu
 void launch_shade(uint32_t n, const uint32_t* nb, const float4* color, const float4* rad, const float4* illum,
                   float* colors, float* radiative, cudaStream_t s);

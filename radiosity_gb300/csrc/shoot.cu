@@ -615,4 +615,28 @@ void launch_areas(const float* verts, uint32_t n, float* area, cudaStream_t s) {
     k_areas<<<(n + 255) / 256, 256, 0, s>>>(verts, n, area);
 }
 
+// The host's per-patch float3 arrays (ModelContainer's AoS layout) arrive by one DMA into a
+// device scratch and are widened here to the solver's float4 rows (w = 0), and back.
+__global__ void k_f3_to_f4(const float* __restrict__ src, float4* __restrict__ dst, uint32_t n) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+        dst[p] = make_float4(src[3 * (size_t)p], src[3 * (size_t)p + 1], src[3 * (size_t)p + 2], 0.f);
+}
+
+__global__ void k_f4_to_f3(const float4* __restrict__ src, float* __restrict__ dst, uint32_t n) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const float4 v = src[p];
+        dst[3 * (size_t)p] = v.x;
+        dst[3 * (size_t)p + 1] = v.y;
+        dst[3 * (size_t)p + 2] = v.z;
+    }
+}
+
+void launch_f3_to_f4(const float* src, float4* dst, uint32_t n, cudaStream_t s) {
+    k_f3_to_f4<<<152 * 4, 256, 0, s>>>(src, dst, n);
+}
+
+void launch_f4_to_f3(const float4* src, float* dst, uint32_t n, cudaStream_t s) {
+    k_f4_to_f3<<<152 * 4, 256, 0, s>>>(src, dst, n);
+}
+
 }  // namespace rad

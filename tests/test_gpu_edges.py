@@ -103,3 +103,26 @@ def test_empty_scene_is_rejected(lib):
         with pytest.raises(lib.RadError) as e:
             s.shoot(1)
         assert e.value.status == -4
+
+
+def test_state_round_trip_through_caller_buffers(lib, small):
+    """rad_set_state / rad_download with caller-owned host buffers: fresh pageable arrays
+    (pages never touched), reused arrays and page-locked arrays give the same bits."""
+    torch = pytest.importorskip("torch")
+    n = small["n"]
+    rng = np.random.default_rng(8)
+    rad = rng.random(3 * n).astype(np.float32)
+    ill = rng.random(3 * n).astype(np.float32)
+    with solver(lib, small, 16, 4) as s:
+        s.set_state(radiosity=rad, illumination=ill)
+        r0, i0 = s.download()
+        assert np.array_equal(_bits(r0), _bits(rad)) and np.array_equal(_bits(i0), _bits(ill))
+        fresh = (np.empty(3 * n, np.float32), np.empty(3 * n, np.float32))
+        s.download(out=fresh)
+        pinned = tuple(torch.empty(3 * n, dtype=torch.float32, pin_memory=True).numpy() for _ in range(2))
+        s.download(out=pinned)
+        for a, b in ((fresh, (r0, i0)), (pinned, (r0, i0))):
+            assert np.array_equal(_bits(a[0]), _bits(b[0])) and np.array_equal(_bits(a[1]), _bits(b[1]))
+        s.set_state(radiosity=pinned[1], illumination=pinned[0])  # pinned sources
+        r1, i1 = s.download()
+        assert np.array_equal(_bits(r1), _bits(ill)) and np.array_equal(_bits(i1), _bits(rad))
