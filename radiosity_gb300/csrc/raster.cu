@@ -785,10 +785,13 @@ __device__ __forceinline__ void hash_add(uint32_t* h_id, unsigned long long* h_s
 // A = v0->v1, v1->v2, v2->v0 and B = v0->v2, v2->v3, v3->v0, each with its own
 // top-left flag.  Each is tracked as f = E + tl - 1, so "inside" (E > 0, or E == 0 on
 // a top-left edge) is f >= 0 and a triangle covers the pixel iff the OR of its three
-// f is >= 0; a triangle absent from the record has one f pinned at -1.  A pixel inside
-// both (possible only where a record's snapped outline folds over) takes the smaller
-// key, as two separate draws would.  The record's fields are copied to registers
-// first: the atomics write shared memory, so reads through `t` would be repeated.
+// f is >= 0; a triangle absent from the record has one f pinned at -1.  B's diagonal
+// v0->v2 is not tracked: its E is exactly -E of A's v2->v0, and exactly one of the two
+// is top-left (a present triangle has v0 != v2: zero-area triangles are culled), so its
+// f is ~f(v2->v0).  A pixel inside both triangles (possible only where a record's
+// snapped outline folds over) takes the smaller key, as two separate draws would.  The
+// record's fields are copied to registers first: the atomics write shared memory, so
+// reads through `t` would be repeated.
 template <int TILE>
 __device__ __forceinline__ void raster_small(const RQuad& t, int x0, int x1, int y0, int start, int steps,
                                              const BinInfo& bi, int sx, int sy, unsigned long long* key) {
@@ -798,11 +801,12 @@ __device__ __forceinline__ void raster_small(const RQuad& t, int x0, int x1, int
     const float c0a = t.c0[0], axa = t.ax[0], aya = t.ay[0];
     const float c0b = t.c0[1], axb = t.ax[1], ayb = t.ay[1];
     const uint32_t id = t.id, flags = t.flags;
-    int32_t f[6], st[6], rs[6];
+    // f[0..2]: A's edges v0->v1, v1->v2, v2->v0; f[3], f[4]: B's edges v2->v3, v3->v0
+    int32_t f[5], st[5], rs[5];
 #pragma unroll
-    for (int k = 0; k < 6; k++) {
-        const int a = k == 0 ? 0 : (k == 1 ? 1 : (k == 2 ? 2 : (k == 3 ? 0 : (k == 4 ? 2 : 3))));  // from
-        const int j = k == 0 ? 1 : (k == 1 ? 2 : (k == 2 ? 0 : (k == 3 ? 2 : (k == 4 ? 3 : 0))));  // to
+    for (int k = 0; k < 5; k++) {
+        const int a = k == 0 ? 0 : (k == 1 ? 1 : (k == 2 ? 2 : (k == 3 ? 2 : 3)));  // from
+        const int j = k == 0 ? 1 : (k == 1 ? 2 : (k == 2 ? 0 : (k == 3 ? 3 : 0)));  // to
         const int32_t dx = t.X[j] - t.X[a], dy = t.Y[j] - t.Y[a];
         const bool tl = (t.Y[j] < t.Y[a]) || (t.Y[j] == t.Y[a] && t.X[j] < t.X[a]);
         f[k] = dx * (py * 256 + 128 - t.Y[a]) - dy * (px * 256 + 128 - t.X[a]) - (tl ? 0 : 1);
@@ -814,7 +818,7 @@ __device__ __forceinline__ void raster_small(const RQuad& t, int x0, int x1, int
     int idx = (py - bi.y0) * TILE + (px - bi.x0);
     const int rowjump = TILE - (w - 1);
     for (int i = 0; i < steps; i++) {
-        const int32_t ca = f[0] | f[1] | f[2], cb = f[3] | f[4] | f[5];
+        const int32_t ca = f[0] | f[1] | f[2], cb = ~f[2] | f[3] | f[4];
         if ((ca & cb) >= 0) {
             // one plane per lane (A when inside A, else B), so the warp evaluates one depth
             const bool ina = ca >= 0;
@@ -832,7 +836,7 @@ __device__ __forceinline__ void raster_small(const RQuad& t, int x0, int x1, int
         py += wrap ? 1 : 0;
         idx += wrap ? rowjump : 1;
 #pragma unroll
-        for (int k = 0; k < 6; k++) f[k] += wrap ? rs[k] : st[k];
+        for (int k = 0; k < 5; k++) f[k] += wrap ? rs[k] : st[k];
     }
 }
 
