@@ -190,6 +190,13 @@ int rad_gather_residual(rad_ctx* ctx, const float* emission, uint32_t R, const f
  * reciprocity error, so each method is checked against its own system. */
 int rad_shoot_residual(rad_ctx* ctx, const float* emission, uint32_t R, const float* radiosity, float* residual);
 
+/* Self-test of the device-side failure path: a kernel waits on an mbarrier that nothing
+ * completes, with the bound every pipeline wait of this library has (limit_us here, 2 s in
+ * the solver kernels).  Returns RAD_E_TIMEOUT once the wait has given up and the kernel has
+ * returned (the expected outcome), with the measured wall time in *waited_ms (may be NULL);
+ * the device stays usable.  limit_us in 1..2,000,000. */
+int rad_selftest_bounded_wait(int device, uint32_t limit_us, double* waited_ms);
+
 /* Diagnostic: C = A * Bt^T on the tcgen05 path (A n x k, Bt R x k BF16 bits, row-major;
  * C column-major R x n FP32), on `device`. */
 int rad_bf16_gemm(int device, const uint16_t* A, const uint16_t* Bt, uint32_t n, uint32_t k, uint32_t R, float* C);

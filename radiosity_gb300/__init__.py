@@ -8,7 +8,7 @@ with ctypes.  Scene generators for the synthetic benchmark workloads live in
 from ._lib import (  # noqa: F401
     EXPORTS, MLP, MODE_PHYS, MODE_REF, Multi, RadConfig, RadError, RadGatherStats, RadStats, RadTuning, Solver, bf16_gemm,
     default_config, derived, load, obj_scene, plan_shooters, reference_neighbours,
-    reference_scene, rr_read, rr_write,
+    reference_scene, rr_read, rr_write, selftest_bounded_wait,
 )
 from .build import LIB as LIB_PATH  # noqa: F401
 from .build import build  # noqa: F401

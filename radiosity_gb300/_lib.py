@@ -39,7 +39,7 @@ EXPORTS = [
     "rad_mlp_train", "rad_multi_create", "rad_multi_shoot", "rad_multi_destroy", "rad_strerror", "rad_last_error",
     "rad_scene_reference_neighbours", "rad_scene_obj", "rad_rr_size", "rad_rr_write", "rad_rr_read",
     "rad_upload_neighbours", "rad_display_colors", "rad_display_colors_device", "rad_highest_patch", "rad_progress",
-    "rad_set_progress",
+    "rad_set_progress", "rad_selftest_bounded_wait",
 ]
 STAGES = ["select", "camera", "setup", "bins", "raster", "update", "emitters"]
 STAGE_KERNELS = [1, 1, 1, 2, 1, 1, 1]
@@ -137,6 +137,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rad_gather_residual.argtypes = [vp, _f32p, ctypes.c_uint32, _f32p, _f32p]
     L.rad_shoot_residual.argtypes = [vp, _f32p, ctypes.c_uint32, _f32p, _f32p]
     L.rad_bf16_gemm.argtypes = [ctypes.c_int, vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _f32p]
+    L.rad_selftest_bounded_wait.argtypes = [ctypes.c_int, ctypes.c_uint32, P(ctypes.c_double)]
     L.rad_mlp_create.argtypes = [ctypes.c_int, ctypes.c_uint64, P(vp)]
     L.rad_mlp_destroy.argtypes = [vp]
     L.rad_mlp_param_count.argtypes = []
@@ -284,6 +285,15 @@ def rr_read(data: bytes) -> dict:
     out["n"] = n.value
     out["pointer_bytes"] = ptr.value
     return out
+
+
+def selftest_bounded_wait(limit_us: int, device: int = 0):
+    """rad_selftest_bounded_wait: (status, waited_ms) of a device wait that nothing completes;
+    the expected status is RAD_E_TIMEOUT."""
+    L = load()
+    ms = ctypes.c_double(0.0)
+    rc = L.rad_selftest_bounded_wait(device, limit_us, ctypes.byref(ms))
+    return rc, ms.value
 
 
 def bf16_gemm(A_bits: np.ndarray, Bt_bits: np.ndarray, device: int = 0) -> np.ndarray:

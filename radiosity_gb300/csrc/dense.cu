@@ -192,8 +192,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
 }
 
-// Waits for the phase of the given parity; false (and the error word, when given, set) after kWaitNs.
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, uint32_t* err) {
+// Waits for the phase of the given parity; false (and the error word, when given, set) after
+// limit_ns of global time.
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, uint32_t* err,
+                                          unsigned long long limit_ns = kWaitNs) {
     const uint32_t a = smem_u32(b);
     unsigned long long t0 = 0;
     for (uint32_t it = 0;; it++) {
@@ -207,12 +209,29 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, uint32_t
         if ((it & 255u) == 0) {
             const unsigned long long t = global_ns();
             if (it == 0) t0 = t;
-            else if (t - t0 > kWaitNs) {
+            else if (t - t0 > limit_ns) {
                 if (err) atomicOr(err, 1u);
                 return false;
             }
         }
     }
+}
+
+// Self-test of the bounded pipeline wait: one thread waits on an mbarrier that nothing
+// arrives on.  The wait gives up after limit_ns and sets *err, which is the path every
+// pipeline wait takes when its copies never land; the kernel then returns normally.
+__global__ void k_wait_selftest(uint32_t* err, unsigned long long limit_ns) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mbar_wait(&bar, 0, err, limit_ns);
+    }
+}
+
+int launch_wait_selftest(uint32_t* err, unsigned long long limit_ns, cudaStream_t s) {
+    k_wait_selftest<<<1, 32, 0, s>>>(err, limit_ns);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 // ---------------------------------------------------------------------------

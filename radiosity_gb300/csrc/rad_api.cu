@@ -1095,6 +1095,39 @@ int rad_shoot_residual(rad_ctx* c, const float* emission, uint32_t R, const floa
     return rc;
 }
 
+int rad_selftest_bounded_wait(int device, uint32_t limit_us, double* waited_ms) {
+    if (limit_us == 0 || limit_us > 2000000u) return RAD_E_INVALID;
+    if (cudaSetDevice(device) != cudaSuccess) return RAD_E_CUDA;
+    uint32_t* derr = nullptr;
+    if (cudaMalloc(&derr, 4) != cudaSuccess) return RAD_E_NOMEM;
+    cudaStream_t s = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = RAD_OK;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+        cudaEventCreate(&e1) != cudaSuccess)
+        rc = RAD_E_CUDA;
+    uint32_t herr = 0;
+    if (!rc) {
+        cudaMemsetAsync(derr, 0, 4, s);
+        cudaEventRecord(e0, s);
+        if (launch_wait_selftest(derr, 1000ull * limit_us, s) != 0) rc = RAD_E_CUDA;
+        cudaEventRecord(e1, s);
+        cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) rc = RAD_E_CUDA;
+    }
+    if (!rc) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (waited_ms) *waited_ms = ms;
+        rc = herr ? RAD_E_TIMEOUT : RAD_OK;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (s) cudaStreamDestroy(s);
+    cudaFree(derr);
+    return rc;
+}
+
 int rad_bf16_gemm(int device, const uint16_t* A, const uint16_t* Bt, uint32_t n, uint32_t k, uint32_t R, float* C) {
     if (!A || !Bt || !C || n == 0 || k == 0 || R == 0) return RAD_E_INVALID;
     const uint32_t Rpad = gemm_tc_width(R);

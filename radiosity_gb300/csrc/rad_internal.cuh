@@ -164,6 +164,8 @@ void launch_dense_rows(unsigned long long* Fq, uint32_t count, uint32_t n, uint3
 // sgemm_resid_scratch_floats(R, ld) floats (0 for larger R: scratch may be null) and sets
 // *err (when given) if one of its bounded pipeline waits timed out.
 size_t sgemm_resid_scratch_floats(uint32_t R, uint32_t ld);
+// One bounded mbarrier wait that nothing completes: sets *err after limit_ns.
+int launch_wait_selftest(uint32_t* err, unsigned long long limit_ns, cudaStream_t s);
 void launch_sgemm_resid(const float* F, uint32_t n, uint32_t ld, const float* X, const float* E, const float4* rho,
                         uint32_t R, float* r, double* nrm, float* scratch, uint32_t* err, cudaStream_t s);
 void launch_shoot_resid(const float* F, uint32_t n, uint32_t ld, const float* X, const float* E, const float4* rho,

@@ -126,3 +126,16 @@ def test_state_round_trip_through_caller_buffers(lib, small):
         s.set_state(radiosity=pinned[1], illumination=pinned[0])  # pinned sources
         r1, i1 = s.download()
         assert np.array_equal(_bits(r1), _bits(ill)) and np.array_equal(_bits(i1), _bits(rad))
+
+
+def test_bounded_device_wait_gives_up_and_the_device_stays_usable(lib, small):
+    """The failure path of every pipeline wait (tcgen05 GEMM, streaming residual): a wait on
+    an mbarrier that nothing completes gives up after its bound, the kernel returns, the host
+    reads RAD_E_TIMEOUT, and the device keeps working."""
+    rc, ms = lib.selftest_bounded_wait(50_000)  # 50 ms
+    assert rc == lib._lib.RAD_E_TIMEOUT
+    assert 45.0 <= ms < 2000.0
+    with solver(lib, small, 16, 4) as s:  # a full shoot afterwards still runs
+        st = s.shoot(2)
+        assert st.shots_done == 2
+    assert lib.selftest_bounded_wait(0)[0] == lib._lib.RAD_E_INVALID
