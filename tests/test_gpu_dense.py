@@ -177,3 +177,27 @@ def test_gather_ignores_leftover_device_memory(lib, box):
             torch.cuda.empty_cache()
             B, st = s.gather(E, tol=1e-6, max_outer=60, sweeps=6)
             assert st.residual <= 1e-6 and np.all(np.isfinite(B))
+
+
+def test_streaming_residual_over_many_stages(lib):
+    """k_resid_stream on a scene wide enough that its 3-stage ring wraps many times (N ~ 4k:
+    8 stages of 512 columns per row block) and rows do not fill the last CTA: the residual
+    equals an FP64 evaluation on the same FP32 rows within 1e-6 of the terms' size."""
+    from radiosity_gb300 import scenes
+
+    sc = scenes.room_with_boxes(target=4000, seed=33)
+    n = sc["n"]
+    rng = np.random.default_rng(7)
+    E = rng.uniform(0, 5, (3, n)).astype(np.float32)
+    B = rng.uniform(0, 10, (3, n)).astype(np.float32)
+    with _solver(lib, sc) as s:
+        s.dense_capture(keep_fp32=True)
+        F, _, _ = s.dense_rows(0, n)
+        r = s.gather_residual(E, B)
+    rho = sc["reflectance"].reshape(n, 3).astype(np.float64)
+    F64 = F.astype(np.float64)
+    for c in range(3):
+        rc = rho[:, c]
+        ref = E[c] + rc * (F64 @ B[c].astype(np.float64)) - B[c]
+        size = np.abs(E[c]) + rc * (np.abs(F64) @ np.abs(B[c].astype(np.float64))) + np.abs(B[c])
+        assert np.all(np.abs(r[c] - ref) <= 1e-6 * size), c
