@@ -8,14 +8,20 @@ all patches.  Metric: hemicubes/s (higher is better).
 
   value    device time of the timed steps (CUDA events on the solver stream),
            scene resident in HBM, one CUDA-graph replay per step
-  e2e      the same steps through the C ABI with host buffers: per step the
-           unshot/shot state is copied host->device, one batch runs, the state is
-           copied back device->host, all inside the timed region
+  e2e      the same steps through the C ABI with host buffers (page-locked when
+           torch is importable, reused every step): per step the unshot/shot state
+           is copied host->device, one batch runs, the state is copied back
+           device->host, all inside the timed region
   roofline the hemicube raster + reduce kernel (the dominant kernel), timed live
            with CUDA events between stages on the solver stream
   cpu_baseline  the CPU oracle (a C port of the reference's shoot loop with a
            software rasteriser) on a bounded sample of the same workload, all host
            threads
+
+Other configurations: ``--workload small`` (5k-patch Cornell box, W=256, K=10),
+``precision`` (20k patches, 192 right-hand sides, gather to 1e-6), ``learned`` (trains the
+warm-start network on 2,000 generated scenes, evaluates on 100 held-out 50k-patch rooms;
+several minutes) and ``uneven`` (256 scenes under one CUDA graph, then learned + gather).
 
 ``--impl reference`` times the reference's CPU path (the oracle port: the
 reference's own GL/CL path cannot run without a graphics stack) on the same
