@@ -73,7 +73,7 @@ int rad_create(const rad_config* cfg, rad_ctx** out);
 int rad_destroy(rad_ctx* ctx);
 
 /* Uploads the scene of ModelContainer::getVertices/getIndices/getPatches
- * (source/ModelContainer.cpp:135-209): vertices N*12 floats (4 corners per patch),
+ * (source/ModelContainer.cpp:161-219): vertices N*12 floats (4 corners per patch),
  * indices N*6 (may be NULL; if given it must be the (0,1,2,0,2,3)+4i pattern),
  * color N*3 (Patch::getColor), reflectance N*3 (PHYS only, may be NULL in REF),
  * radiosity N*3 (Patch::radiosity = unshot energy), illumination N*3. */
@@ -91,7 +91,7 @@ int rad_download(rad_ctx* ctx, float* radiosity, float* illumination);
  * texture-layout tables, 2W x 1.5W floats each, written to out. */
 int rad_ff_table(rad_ctx* ctx, float* out, uint32_t copies);
 
-/* ModelContainer::getHighestRadiosityPatchesId (source/ModelContainer.cpp:313-353) on
+/* ModelContainer::getHighestRadiosityPatchesId (source/ModelContainer.cpp:259-299) on
  * the device-resident state: K ids and validity flags (valid[k]==0 <=> NULL emitter).
  * PHYS mode selects the K largest unshot powers instead. */
 int rad_select_shooters(rad_ctx* ctx, uint32_t* ids, uint8_t* valid);
@@ -242,7 +242,7 @@ int rad_multi_destroy(rad_multi* m);
  * inside, big-triangle pixels written. */
 int rad_raster_counters(rad_ctx* ctx, uint64_t* out);
 
-/* Builds the reference scene (ModelContainer::load, source/ModelContainer.cpp:89-110,
+/* Builds the reference scene (ModelContainer::load, source/ModelContainer.cpp:35-56,
  * PrimitiveModel ROOM/ROOMCLOSURE/CUBE/BLOCK subdivided to max_patch_area).  Call with
  * NULL arrays to get *n; then again with arrays of capacity >= *n patches. */
 int rad_scene_reference(double max_patch_area, uint32_t capacity, uint32_t* n, float* vertices,

@@ -115,7 +115,7 @@ class ModelContainer {
         if (ctx) rad_destroy(ctx);
         for (Patch* p : patches) delete p;
     }
-    // ROOM + ROOMCLOSURE + CUBE + BLOCK of source/ModelContainer.cpp:89-110 (built lazily).
+    // ROOM + ROOMCLOSURE + CUBE + BLOCK of source/ModelContainer.cpp:35-56 (built lazily).
     void load() { loaded = true; }
     float* getVertices() { return refresh(), vertices.data(); }
     unsigned getVerticesCount() { return refresh(), (unsigned)vertices.size(); }

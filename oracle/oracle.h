@@ -40,7 +40,7 @@ void orc_face_rects(uint32_t W, uint32_t hi, int face, int vp[4], int sc[4]);
 
 /* Column-major MVP (out[col*4+row]) of face `face` looking from quad q (12
  * floats), restating Camera::lookFromPatch, CGLTransform::LookAt/Perspective/
- * Frustum and Matrix4f products (source/Camera.cpp:54-87,132-138,
+ * Frustum and Matrix4f products (source/Camera.cpp:19-52,97-103,
  * source/Transform.cpp:26-80,127-156, source/Vector.cpp:445-527,
  * source/Main.cpp:1170-1183). */
 void orc_face_mvp(const float* q, int face, float* out);
@@ -51,7 +51,7 @@ void orc_patch_frame(const float* q, float* out9);
 /* Item buffer of one hemicube: 2W x 1.5W uint32, 0 = nothing, else patch+1.
  * Local (hemicube-relative) window coordinates are used, so the result does not
  * depend on the hemicube's slot in a batch.  Rules (the raster contract):
- *  - quad p = triangles (v0,v1,v2),(v0,v2,v3) (source/ModelContainer.cpp:166-171)
+ *  - quad p = triangles (v0,v1,v2),(v0,v2,v3) (source/ModelContainer.cpp:112-117)
  *  - patches with all 4 vertices strictly behind the shooter plane are skipped
  *  - clip space c_r = ((m0r*x + m1r*y) + m2r*z) + m3r
  *  - Sutherland-Hodgman clip against z+w>=0, w-z>=0, 1024w-x>=0, 1024w+x>=0,
@@ -82,7 +82,7 @@ void orc_ff_from_records(uint32_t k, uint32_t n, uint32_t nrec, const uint32_t* 
 void orc_ff_exact(uint32_t W, uint32_t k, uint32_t n, const uint32_t* items, float* F);
 
 /* Top-K selection of ModelContainer::getHighestRadiosityPatchesId
- * (source/ModelContainer.cpp:313-353), simulated literally (list append, stable
+ * (source/ModelContainer.cpp:259-299), simulated literally (list append, stable
  * ascending sort, reverse, truncate).  rad is n*3; ids[k], valid[k]. */
 void orc_topk_ref(const float* rad, uint32_t n, uint32_t K, uint32_t* ids, uint8_t* valid);
 

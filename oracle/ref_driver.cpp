@@ -4,9 +4,9 @@
 // reference's shoot loop does and copies results into flat arrays so that the
 // pytest suite (via ctypes) can pin the oracle restatement and the product's
 // host-side code against it:
-//   ref_scene_*      ModelContainer::load + updateData      (source/ModelContainer.cpp:89-209)
+//   ref_scene_*      ModelContainer::load + updateData      (source/ModelContainer.cpp:35-56,81-155)
 //   ref_ff_table     precomputeHemicubeFormFactors           (source/FormFactors.cpp:280-339)
-//   ref_topk         ModelContainer::getHighestRadiosityPatchesId (source/ModelContainer.cpp:313-353)
+//   ref_topk         ModelContainer::getHighestRadiosityPatchesId (source/ModelContainer.cpp:259-299)
 //   ref_face_mvp     the per-face MVP of the shoot loop      (source/Main.cpp:1166-1184)
 //   ref_config_*     Config::freeze and its getters          (source/Config.cpp:30-48)
 //   ref_neighbours   Patch::neighbours as scene indices      (source/Patch.cpp:128-219)

@@ -1,7 +1,7 @@
 // Hemicube face cameras on the device.
 //
 // Follows, operation for operation, Patch::getCenter/getNormal/getUp
-// (source/Patch.cpp:253-276), Camera::lookFromPatch (source/Camera.cpp:54-87),
+// (source/Patch.cpp:253-276), Camera::lookFromPatch (source/Camera.cpp:19-52),
 // CGLTransform::LookAt (source/Transform.cpp:127-156) and the Matrix4f products
 // (source/Vector.cpp:445-527) as used by the shoot loop (source/Main.cpp:1170-1183).
 // The library is compiled with -fmad=false and IEEE division / square root, so

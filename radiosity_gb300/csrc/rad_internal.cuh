@@ -23,7 +23,7 @@ constexpr int kMaxK = 1024;
 
 // One rasterisable record: up to two triangles of one patch that share vertex 0,
 // A = (v0, v1, v2) and B = (v0, v2, v3).  An unclipped patch quad is one record (its
-// two triangles, source/ModelContainer.cpp:166-171); a clipped triangle's fan is
+// two triangles, source/ModelContainer.cpp:112-117); a clipped triangle's fan is
 // packed two triangles per record.  Hemicube-local 24.8 fixed-point window coordinates.
 // Each triangle keeps its own depth plane; the plane's constant term is rebuilt from
 // d0 exactly as it was computed: c0 = (d0 + gx*ox) + gy*oy with gx = ax / 256.

@@ -1,5 +1,5 @@
 // Host-side scene builders and scene files of the reference:
-//  * the reference scene: ModelContainer::load (source/ModelContainer.cpp:89-110)
+//  * the reference scene: ModelContainer::load (source/ModelContainer.cpp:35-56)
 //    = PrimitiveModel ROOM, ROOMCLOSURE, CUBE, BLOCK (source/PrimitiveModel.cpp:4-213),
 //    each subdivided once by Model::subdivide / Patch::divide
 //    (source/Model.cpp:27-60, source/Patch.cpp:47-222) and flattened by
@@ -49,7 +49,7 @@ void self_neighbours(Quad& q, uint32_t self) {
     for (int j = 0; j < 8; j++) q.nb[j] = self;
 }
 
-// x y z of 4 corners per quad, 5 quads per part (source/PrimitiveModel.cpp:132-245).
+// x y z of 4 corners per quad, 5 quads per part (source/PrimitiveModel.cpp:4-213).
 const float kRoom[60] = {0.0f, 0.0f, 5.592f, 5.496f, 0.0f, 5.592f, 5.560f, 5.488f, 5.592f, 0.0f, 5.488f, 5.592f,
                          0.0f, 5.488f, 0.0f, 0.0f, 5.488f, 5.592f, 5.560f, 5.488f, 5.592f, 5.560f, 5.488f, 0.0f,
                          0.0f, 0.0f, 0.0f, 5.528f, 0.0f, 0.0f, 5.496f, 0.0f, 5.592f, 0.0f, 0.0f, 5.592f,

@@ -1,6 +1,6 @@
 // Shooting step on the device: shooter selection, radiosity update, emitter
 // update and the stop rule (source/Main.cpp:1137-1303,
-// source/ModelContainer.cpp:313-353).
+// source/ModelContainer.cpp:259-299).
 //
 // Selection (one CTA).  The reference keeps a std::list of at most K patch ids:
 // patch 0 is always inserted; patch i>0 is inserted when |B_i|^2 > 0 and
