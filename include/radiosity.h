@@ -84,7 +84,10 @@ int rad_upload_scene(rad_ctx* ctx, const float* vertices, const int32_t* indices
 /* Replaces the radiosity / illumination state (either may be NULL to keep it). */
 int rad_set_state(rad_ctx* ctx, const float* radiosity, const float* illumination);
 
-/* Copies Patch::radiosity and Patch::illumination (N*3 each; either may be NULL). */
+/* Copies Patch::radiosity and Patch::illumination (N*3 each; either may be NULL).  The
+ * arrays must be writable host memory; pageable arrays have one byte per page read and
+ * written back unchanged before the copy (it populates the pages), so a failed call leaves
+ * their contents as they were. */
 int rad_download(rad_ctx* ctx, float* radiosity, float* illumination);
 
 /* precomputeHemicubeFormFactors (source/FormFactors.cpp:280-339): `copies` stacked
@@ -106,6 +109,14 @@ int rad_reduce_item_buffers(rad_ctx* ctx, const uint32_t* items, uint32_t count,
 
 /* Render + reduce fused: count x N form-factor rows of the given shooters. */
 int rad_ff_rows(rad_ctx* ctx, const uint32_t* shooters, uint32_t count, float* ff_rows);
+
+/* The hemicube cameras of `count` shooters (1..1024) as the draw uses them:
+ * Camera::lookFromPatch (source/Camera.cpp:19-52) for the faces UP, DOWN, LEFT, RIGHT,
+ * FRONT, each view matrix multiplied by Perspective(90, 1, 0.01, 1000)
+ * (source/Main.cpp:1166-1184).  mvp receives count x 5 column-major 4x4 matrices; frames
+ * (may be NULL) receives count x 6 floats, Patch::getCenter then Patch::getNormal
+ * (source/Patch.cpp:261-276). */
+int rad_face_cameras(rad_ctx* ctx, const uint32_t* shooters, uint32_t count, float* mvp, float* frames);
 
 /* Runs up to n_shots batches of the shoot loop (source/Main.cpp:1137-1309) on the
  * device-resident state, K = hemicubes_count shooters per batch; stops early on the
@@ -313,8 +324,8 @@ int rad_set_progress(rad_ctx* ctx, uint32_t shots_done, double initial_power);
  * the caller's DEVICE buffers: d_items holds `count` stacked 2W x 1.5W uint32 item
  * buffers (0 = nothing, else patch index + 1; ids above n_patches are ignored) and
  * d_ff_rows receives count x n_patches floats, the same values rad_reduce_item_buffers
- * returns.  `stream` is a cudaStream_t (NULL = default stream); the call returns after
- * the stream has finished the work.  No rad_ctx, no cudaMalloc/cudaFree: the only
+ * returns.  `stream` is a cudaStream_t (NULL = default stream); the call waits for the
+ * stream to finish (cudaStreamSynchronize) before it returns.  No rad_ctx, no cudaMalloc/cudaFree: the only
  * scratch is a fixed device array of RAD_NOALLOC_MAX_SUMS 64-bit sums (8 MiB) that every
  * GPU loading the library holds until exit, so count * n_patches must not exceed
  * RAD_NOALLOC_MAX_SUMS (else RAD_E_NOALLOC_LIMIT).  The first call on a device looks the

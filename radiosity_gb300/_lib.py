@@ -39,7 +39,7 @@ EXPORTS = [
     "rad_mlp_train", "rad_multi_create", "rad_multi_shoot", "rad_multi_destroy", "rad_strerror", "rad_last_error",
     "rad_scene_reference_neighbours", "rad_scene_obj", "rad_rr_size", "rad_rr_write", "rad_rr_read",
     "rad_upload_neighbours", "rad_display_colors", "rad_display_colors_device", "rad_highest_patch", "rad_progress",
-    "rad_set_progress", "rad_selftest_bounded_wait",
+    "rad_set_progress", "rad_selftest_bounded_wait", "rad_face_cameras",
 ]
 STAGES = ["select", "camera", "setup", "bins", "raster", "update", "emitters"]
 STAGE_KERNELS = [1, 1, 1, 2, 1, 1, 1]
@@ -127,6 +127,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rad_render_item_buffers.argtypes = [vp, _u32p, ctypes.c_uint32, _u32p]
     L.rad_reduce_item_buffers.argtypes = [vp, _u32p, ctypes.c_uint32, _f32p]
     L.rad_ff_rows.argtypes = [vp, _u32p, ctypes.c_uint32, _f32p]
+    L.rad_face_cameras.argtypes = [vp, _u32p, ctypes.c_uint32, _f32p, vp]
     L.rad_shoot.argtypes = [vp, ctypes.c_uint32, P(RadStats)]
     L.rad_profile_stages.argtypes = [vp, ctypes.c_uint32, np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS"),
                                      P(RadStats)]
@@ -453,6 +454,15 @@ class Solver:
         out = np.zeros(s.size * self.n, np.float32)
         self._check(self.L.rad_ff_rows(self.h, s, s.size, out), "rad_ff_rows")
         return out.reshape(s.size, self.n)
+
+    def face_cameras(self, shooters):
+        """Device face MVPs (count x 5 x 16, column-major) and frames (count x 6: center, normal)."""
+        s = np.ascontiguousarray(shooters, np.uint32).reshape(-1)
+        mvp = np.zeros(s.size * 80, np.float32)
+        fr = np.zeros(s.size * 6, np.float32)
+        self._check(self.L.rad_face_cameras(self.h, s, s.size, mvp, fr.ctypes.data_as(ctypes.c_void_p)),
+                    "rad_face_cameras")
+        return mvp.reshape(s.size, 5, 16), fr.reshape(s.size, 6)
 
     def profile_stages(self, n_shots: int):
         """Per-stage device milliseconds (summed over the batches) and the stats."""

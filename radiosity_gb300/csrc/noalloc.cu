@@ -96,24 +96,31 @@ __global__ void k_noalloc_clear(unsigned long long* sums, size_t total) {
         sums[i] = 0;
 }
 
+// Grid-stride over the count * 3W^2 texels; the stride is a whole number of blocks, so the
+// lanes of a warp run the same iterations and the warp-wide match below sees all 32 lanes.
 __global__ void k_noalloc_reduce(const uint32_t* __restrict__ items, uint32_t count, uint32_t W, uint32_t n,
                                  unsigned long long* sums) {
     const uint32_t res = 3 * W * W;
     const size_t total = (size_t)count * res;
-    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
-    const uint32_t it = idx < total ? items[idx] : 0u;
-    const bool has = it != 0 && it <= n;
-    const uint32_t hi = (uint32_t)(idx / res), pix = (uint32_t)(idx % res);
-    unsigned long long q = 0;
-    if (has) q = __float2ull_rz(noalloc_ff(W, pix) * 0x1p61f);
-    const uint32_t key = has ? (it - 1) ^ (hi << 31) : 0xFFFFFFFFu;
-    const unsigned m = __match_any_sync(0xffffffffu, key);
-    const uint32_t a = (uint32_t)(q & 0x1FFFFFull), b = (uint32_t)((q >> 21) & 0x1FFFFFull), c = (uint32_t)(q >> 42);
-    const uint32_t sa = __reduce_add_sync(m, a), sb = __reduce_add_sync(m, b), sc = __reduce_add_sync(m, c);
-    const unsigned long long sum =
-        (unsigned long long)sa + ((unsigned long long)sb << 21) + ((unsigned long long)sc << 42);
-    if (has && lane == __ffs(m) - 1) atomicAdd(&sums[(size_t)hi * n + (it - 1)], sum);
+    for (size_t base = (size_t)blockIdx.x * blockDim.x; base < total; base += (size_t)gridDim.x * blockDim.x) {
+        const size_t idx = base + threadIdx.x;
+        const uint32_t it = idx < total ? items[idx] : 0u;
+        const bool has = it != 0 && it <= n;
+        const uint32_t hi = (uint32_t)(idx / res), pix = (uint32_t)(idx % res);
+        unsigned long long q = 0;
+        if (has) q = __float2ull_rz(noalloc_ff(W, pix) * 0x1p61f);
+        // one warp may span several images (12 texels each at W = 2): the key holds the image
+        // index and the patch id
+        const unsigned long long key = has ? ((unsigned long long)hi << 32) | (it - 1) : ~0ull;
+        const unsigned m = __match_any_sync(0xffffffffu, key);
+        const uint32_t a = (uint32_t)(q & 0x1FFFFFull), b = (uint32_t)((q >> 21) & 0x1FFFFFull),
+                       c = (uint32_t)(q >> 42);
+        const uint32_t sa = __reduce_add_sync(m, a), sb = __reduce_add_sync(m, b), sc = __reduce_add_sync(m, c);
+        const unsigned long long sum =
+            (unsigned long long)sa + ((unsigned long long)sb << 21) + ((unsigned long long)sc << 42);
+        if (has && lane == __ffs(m) - 1) atomicAdd(&sums[(size_t)hi * n + (it - 1)], sum);
+    }
 }
 
 __global__ void k_noalloc_to_float(const unsigned long long* __restrict__ sums, size_t total, float* out) {
@@ -134,8 +141,9 @@ extern "C" int rad_reduce_items_noalloc(const uint32_t* d_items, uint32_t count,
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const size_t pixels = (size_t)count * 3 * hemicube_side * hemicube_side;
     k_noalloc_clear<<<152 * 4, 256, 0, s>>>(scratch, sums);
-    k_noalloc_reduce<<<(unsigned)((pixels + 255) / 256), 256, 0, s>>>(d_items, count, hemicube_side, n_patches,
-                                                                      scratch);
+    const size_t blocks = (pixels + 255) / 256;
+    const unsigned grid = blocks < (size_t)152 * 64 ? (unsigned)blocks : 152u * 64u;  // grid-stride beyond
+    k_noalloc_reduce<<<grid, 256, 0, s>>>(d_items, count, hemicube_side, n_patches, scratch);
     k_noalloc_to_float<<<152 * 4, 256, 0, s>>>(scratch, sums, d_ff_rows);
     if (cudaGetLastError() != cudaSuccess) return RAD_E_CUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return RAD_E_CUDA;

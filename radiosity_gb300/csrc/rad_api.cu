@@ -494,8 +494,8 @@ int rad_set_state(rad_ctx* c, const float* radiosity, const float* illumination)
 // Where the GPU reaches host memory through the host's page tables (NVLink-C2C systems), a
 // copy into never-touched pages faults each page in from the GPU side: measured on GB300,
 // 155 us for a 606 KB array of fresh 64 KB pages, against ~49 us when the CPU populates them
-// first.  Pinned or registered memory is left alone.  The bytes written are overwritten by
-// the copy.
+// first.  Pinned or registered memory is left alone.  Each touched byte is written back with
+// the value it holds, so the caller's array keeps its contents if the copy does not happen.
 static void prefault_pageable(void* p, size_t bytes) {
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
@@ -505,8 +505,8 @@ static void prefault_pageable(void* p, size_t bytes) {
     if (a.type != cudaMemoryTypeUnregistered) return;
     static const size_t page = (size_t)sysconf(_SC_PAGESIZE);
     volatile char* b = static_cast<volatile char*>(p);
-    for (size_t o = 0; o < bytes; o += page) b[o] = 0;
-    if (bytes) b[bytes - 1] = 0;
+    for (size_t o = 0; o < bytes; o += page) b[o] = b[o];
+    if (bytes) b[bytes - 1] = b[bytes - 1];
 }
 
 // Device float4 rows -> the caller's float3 arrays: narrowed on the device into the scratch,
@@ -591,6 +591,33 @@ int rad_ff_rows(rad_ctx* c, const uint32_t* shooters, uint32_t count, float* ff_
     RAD_CUDA(c, cudaMemcpyAsync(ff_rows, c->d_rows, sizeof(float) * (size_t)count * c->n, cudaMemcpyDeviceToHost,
                                 c->stream));
     RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    return RAD_OK;
+}
+
+int rad_face_cameras(rad_ctx* c, const uint32_t* shooters, uint32_t count, float* mvp, float* frames) {
+    if (!c || !mvp) return RAD_E_INVALID;
+    if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
+    if (!shooters || count == 0 || count > (uint32_t)kMaxK) return fail(c, RAD_E_INVALID, "1..1024 shooters");
+    for (uint32_t i = 0; i < count; i++)
+        if (shooters[i] >= c->n) return fail(c, RAD_E_INVALID, "shooter index out of range");
+    int rc = alloc_batch(c, c->aux, count, false);
+    if (rc) return rc;
+    Batch& b = c->aux.b;
+    b.K = count;
+    cudaStream_t s = c->stream;
+    std::vector<uint32_t> ones(count, 1u);
+    RAD_CUDA(c, cudaMemsetAsync(c->d_aux, 0, sizeof(DevState), s));
+    RAD_CUDA(c, cudaMemcpyAsync(b.shooters, shooters, sizeof(uint32_t) * count, cudaMemcpyHostToDevice, s));
+    RAD_CUDA(c, cudaMemcpyAsync(b.valid, ones.data(), sizeof(uint32_t) * count, cudaMemcpyHostToDevice, s));
+    launch_camera(c->geo, b, c->d_verts, c->d_rad, c->d_aux, s);
+    RAD_CUDA(c, cudaGetLastError());
+    std::vector<float> fr((size_t)count * 8);
+    RAD_CUDA(c, cudaMemcpyAsync(mvp, b.mvp, sizeof(float) * 80 * count, cudaMemcpyDeviceToHost, s));
+    RAD_CUDA(c, cudaMemcpyAsync(fr.data(), b.frame, sizeof(float) * 8 * count, cudaMemcpyDeviceToHost, s));
+    RAD_CUDA(c, cudaStreamSynchronize(s));
+    if (frames)
+        for (uint32_t i = 0; i < count; i++)
+            for (int k = 0; k < 6; k++) frames[6 * i + k] = fr[8 * i + k];
     return RAD_OK;
 }
 

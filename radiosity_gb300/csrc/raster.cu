@@ -683,7 +683,7 @@ __device__ __forceinline__ uint32_t depth_ordinal(float d) {
 
 // Exact warp-segmented sum of q over lanes sharing `key`; returns the group's sum
 // on every lane and the group mask in *gm.
-__device__ __forceinline__ unsigned long long group_sum(uint32_t key, unsigned long long q, unsigned* gm) {
+__device__ __forceinline__ unsigned long long group_sum(unsigned long long key, unsigned long long q, unsigned* gm) {
     unsigned m = __match_any_sync(0xffffffffu, key);
     uint32_t a = (uint32_t)(q & 0x1FFFFFull), bb = (uint32_t)((q >> 21) & 0x1FFFFFull), c = (uint32_t)(q >> 42);
     uint32_t sa = __reduce_add_sync(m, a), sb = __reduce_add_sync(m, bb), sc = __reduce_add_sync(m, c);
@@ -1201,10 +1201,11 @@ __global__ void k_reduce_items(Geo g, Batch b, const float* __restrict__ fftab, 
     const uint32_t hi = (uint32_t)(idx / g.RES), pix = (uint32_t)(idx % g.RES);
     unsigned long long q = 0;
     if (has) q = __float2ull_rz(fftab[pix] * 0x1p61f);
-    // lanes of one warp may straddle two images: fold the image into the key
-    const uint32_t key = has ? (it - 1) ^ (hi << 31) : 0xFFFFFFFFu;
+    // the lanes of one warp may span several images (an image is 3W^2 texels: 12 at W = 2),
+    // so the key carries the whole image index beside the patch id
+    const unsigned long long key = has ? ((unsigned long long)hi << 32) | (it - 1) : ~0ull;
     unsigned gm;
-    unsigned long long sum = group_sum(has ? key : 0xFFFFFFFFu, q, &gm);
+    unsigned long long sum = group_sum(key, q, &gm);
     if (has && lane == __ffs(gm) - 1) atomicAdd(&b.Fq[(size_t)hi * g.n + (it - 1)], sum);
 }
 

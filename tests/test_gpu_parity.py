@@ -59,6 +59,16 @@ def test_ff_table_bit_exact(lib, orc, golden, W):
         assert np.array_equal(_bits(t[: ref.size]), _bits(golden[f"ff_table_{W}"]))
 
 
+def test_face_cameras_match_reference_golden(lib, golden, cornell):
+    """Device MVPs and frames of 24 patches against the reference's own Camera::lookFromPatch
+    x Perspective products (golden fixture from the compiled reference)."""
+    pids = np.asarray(golden["mvp_patches"], np.uint32)
+    with solver(lib, cornell, 16, 4) as s:
+        mvp, fr = s.face_cameras(pids)
+    assert np.array_equal(_bits(mvp), _bits(np.asarray(golden["mvp"]).reshape(len(pids), 5, 16)))
+    assert np.array_equal(_bits(fr), _bits(np.asarray(golden["frames"])[:, :6]))
+
+
 @pytest.mark.parametrize("W", [16, 32, 256])
 def test_item_buffers_bit_exact_cornell(lib, orc, cornell, W):
     sh = np.array([light_ids(cornell)[0], 0, 100, 2500, 3000, cornell["n"] - 1], np.uint32)
@@ -90,6 +100,22 @@ def test_reduce_on_identical_item_buffers(lib, orc, cornell):
     nz = Fr > 0
     assert np.array_equal(F > 0, nz)
     assert np.max(np.abs(F[nz] - Fr[nz]) / Fr[nz]) <= REL_FF
+
+
+@pytest.mark.parametrize("W", [2, 4])
+def test_reduce_items_small_hemicubes(lib, orc, cornell, W):
+    """At W=2 an image is 12 texels, so one warp of the reduction spans several images;
+    each image's sums must stay apart (rendered buffers, then ids drawn from 3 patches so
+    that every image holds the same ids)."""
+    n = cornell["n"]
+    sh = [int(light_ids(cornell)[0]), 7, 100, 2500, 4242, 3000]
+    rendered = np.concatenate([orc.render(W, cornell["vertices"], p) for p in sh])
+    rng = np.random.default_rng(W)
+    crowded = rng.integers(0, 4, rendered.size).astype(np.uint32)
+    for items in (rendered, crowded):
+        with solver(lib, cornell, W, len(sh)) as s:
+            F = s.reduce_items(items, len(sh))
+        assert np.array_equal(_bits(F), _bits(orc.ff_exact(W, items, len(sh), n)))
 
 
 @pytest.mark.parametrize("W,tile", [(32, 16), (256, 32), (256, 64)])

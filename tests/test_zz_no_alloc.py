@@ -51,6 +51,22 @@ def test_noalloc_rows_match_context_entry_point(lib, orc):
     assert got2.sum() > 0
 
 
+@pytest.mark.parametrize("W", [2, 4])
+def test_noalloc_rows_small_hemicubes(lib, orc, W):
+    """At W=2 one warp of the reduction spans several 12-texel images: against the
+    oracle's exact rows, on rendered buffers and on buffers whose images all hold the
+    same 3 patch ids."""
+    torch = pytest.importorskip("torch")
+    L = lib.load()
+    sc = lib.reference_scene(0.045)
+    n, count = sc["n"], 6
+    rendered = np.concatenate([orc.render(W, sc["vertices"], p) for p in (0, 7, 100, 2500, 4242, 3000)])
+    crowded = np.random.default_rng(W).integers(0, 4, rendered.size).astype(np.uint32)
+    for items in (rendered, crowded):
+        got = _noalloc_rows(L, torch, items, count, W, n)
+        assert np.array_equal(got.view(np.uint32), orc.ff_exact(W, items, count, n).view(np.uint32))
+
+
 def test_noalloc_rejects_requests_beyond_the_fixed_scratch(lib):
     torch = pytest.importorskip("torch")
     L = lib.load()
