@@ -53,7 +53,7 @@ def parse():
     p.add_argument("--w", type=int, default=512, help="hemicube side")
     p.add_argument("--patches", type=int, default=50000)
     p.add_argument("--tile", type=int, default=0)
-    p.add_argument("--small", type=int, default=0, help="lane/warp triangle split in box pixels (0: default)")
+    p.add_argument("--small", type=int, default=0, help="span/warp record split in box pixels (0: default)")
     p.add_argument("--seed", type=int, default=0)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -276,7 +276,7 @@ def run_ours(args):
             dist.barrier()
 
     tuning = None
-    if not args.no_autotune:  # picks the raster bin side and lane/warp split (state untouched)
+    if not args.no_autotune:  # picks the raster bin side and span/warp split (state untouched)
         t = solver.autotune(tune_k=False)
         tuning = {"tile": t.tile, "small_tri_pixels": t.small_tri_pixels, "candidates": t.candidates,
                   "us_per_hemicube": t.us_per_hemicube}

@@ -42,7 +42,8 @@ typedef struct rad_config {
     uint32_t binref_capacity; /* bin references per hemicube; 0 = 4 * tri_capacity */
     int32_t device;           /* CUDA device ordinal */
     uint32_t small_tri_pixels;/* records whose box clamped to a bin is at most this many pixels (and whose
-                                 extent is at most 64 px) are rasterised by one lane; 0 = 64 */
+                                 extent is at most 64 px) are rasterised by exact row spans, the others
+                                 by one warp per triangle; 1..4096, 0 = 4096 */
 } rad_config;
 
 typedef struct rad_stats {
@@ -142,7 +143,7 @@ int rad_profile_stages(rad_ctx* ctx, uint32_t n_shots, double* stage_ms, rad_sta
 /* Result of rad_autotune. */
 typedef struct rad_tuning {
     uint32_t tile;             /* chosen raster bin side */
-    uint32_t small_tri_pixels; /* chosen lane/warp split */
+    uint32_t small_tri_pixels; /* chosen span/warp split */
     uint32_t hemicubes_count;  /* chosen K (unchanged unless RAD_TUNE_K) */
     uint32_t candidates;       /* configurations timed */
     double us_per_hemicube;    /* render + reduce time of the chosen configuration */
@@ -151,7 +152,7 @@ typedef struct rad_tuning {
 #define RAD_TUNE_K 1u /* also choose K among 8..128 (changes the batching of the solve) */
 
 /* Times the hemicube render + reduce pipeline on the current top shooters for each
- * candidate raster configuration (bin side 16/32/64 x lane/warp split 16..256 px,
+ * candidate raster configuration (bin side 16/32/64 x span/warp split 64..4096 px,
  * optionally K) and reconfigures the context with the fastest.  The radiosity state is
  * not modified.  out may be NULL. */
 int rad_autotune(rad_ctx* ctx, uint32_t flags, rad_tuning* out);
@@ -248,10 +249,18 @@ int rad_multi_shoot(rad_multi* m, uint32_t n_replays, uint32_t* stop_replay, dou
 int rad_multi_destroy(rad_multi* m);
 
 /* Raster counters of the last rad_profile_stages call (8 values): record-bin pairs (a record
- * holds both triangles of a patch quad), small records (one lane each), their box pixels,
- * big records (one warp per triangle), their 8x4 stamps, stamps visited, stamps wholly
- * inside, big-triangle pixels written. */
+ * holds both triangles of a patch quad), small records (row spans), their box pixels, big
+ * records (one warp per triangle), their 8x4 stamps, stamps visited, stamps wholly inside,
+ * big-triangle pixels written. */
 int rad_raster_counters(rad_ctx* ctx, uint64_t* out);
+
+/* Diagnostic twin of rad_profile_stages whose raster kernel also reads the SM clock at its
+ * phase boundaries: runs up to n_shots batches (the state advances as with rad_shoot) and
+ * writes the SM cycles the raster's warps spent per phase, summed over warps, to cycles[8]:
+ * bin set-up, record staging, row ownership, row spans, pixel stream, pass barrier, big
+ * records and chunk barrier, bin end (item buffer / reduction).  The clock reads slow the
+ * raster down by about a fifth, so its stage times are not the kernel's.  stats may be NULL. */
+int rad_profile_raster_phases(rad_ctx* ctx, uint32_t n_shots, uint64_t* cycles, rad_stats* stats);
 
 /* Builds the reference scene (ModelContainer::load, source/ModelContainer.cpp:35-56,
  * PrimitiveModel ROOM/ROOMCLOSURE/CUBE/BLOCK subdivided to max_patch_area).  Call with

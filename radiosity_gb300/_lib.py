@@ -39,7 +39,7 @@ EXPORTS = [
     "rad_mlp_train", "rad_multi_create", "rad_multi_shoot", "rad_multi_destroy", "rad_strerror", "rad_last_error",
     "rad_scene_reference_neighbours", "rad_scene_obj", "rad_rr_size", "rad_rr_write", "rad_rr_read",
     "rad_upload_neighbours", "rad_display_colors", "rad_display_colors_device", "rad_highest_patch", "rad_progress",
-    "rad_set_progress", "rad_selftest_bounded_wait", "rad_face_cameras",
+    "rad_set_progress", "rad_selftest_bounded_wait", "rad_face_cameras", "rad_profile_raster_phases",
 ]
 STAGES = ["select", "camera", "setup", "bins", "raster", "update", "emitters"]
 STAGE_KERNELS = [1, 1, 1, 2, 1, 1, 1]
@@ -128,6 +128,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rad_reduce_item_buffers.argtypes = [vp, _u32p, ctypes.c_uint32, _f32p]
     L.rad_ff_rows.argtypes = [vp, _u32p, ctypes.c_uint32, _f32p]
     L.rad_face_cameras.argtypes = [vp, _u32p, ctypes.c_uint32, _f32p, vp]
+    L.rad_profile_raster_phases.argtypes = [vp, ctypes.c_uint32, np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS"),
+                                            P(RadStats)]
     L.rad_shoot.argtypes = [vp, ctypes.c_uint32, P(RadStats)]
     L.rad_profile_stages.argtypes = [vp, ctypes.c_uint32, np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS"),
                                      P(RadStats)]
@@ -472,7 +474,7 @@ class Solver:
         return dict(zip(STAGES, ms.tolist())), st
 
     def autotune(self, tune_k: bool = False) -> RadTuning:
-        """rad_autotune: picks bin side and lane/warp split (and K when tune_k) by timing."""
+        """rad_autotune: picks bin side and span/warp split (and K when tune_k) by timing."""
         t = RadTuning()
         self._check(self.L.rad_autotune(self.h, 1 if tune_k else 0, ctypes.byref(t)), "rad_autotune")
         self.cfg.tile = t.tile
@@ -524,11 +526,20 @@ class Solver:
 
     RASTER_COUNTERS = ["record_bin_pairs", "small_records", "small_box_px", "big_records", "big_stamps",
                        "stamps_visited", "stamps_inside", "big_px_written"]
+    RASTER_PHASES = ["setup", "stage", "rows", "spans", "pixels", "pass_sync", "big", "end"]
 
     def raster_counters(self) -> dict:
         out = np.zeros(8, np.uint64)
         self._check(self.L.rad_raster_counters(self.h, out), "rad_raster_counters")
         return dict(zip(self.RASTER_COUNTERS, [int(x) for x in out]))
+
+    def raster_phases(self, n_shots: int) -> dict:
+        """SM cycles per raster phase (summed over warps) over n_shots batches (advances the state)."""
+        out = np.zeros(8, np.uint64)
+        st = RadStats()
+        self._check(self.L.rad_profile_raster_phases(self.h, n_shots, out, ctypes.byref(st)),
+                    "rad_profile_raster_phases")
+        return dict(zip(self.RASTER_PHASES, [int(x) for x in out]))
 
     def shoot(self, n_shots: int) -> RadStats:
         st = RadStats()

@@ -187,8 +187,7 @@ static void setup_geo(rad_ctx* c, std::vector<BinInfo>& bins) {
     g.tile = tile;
     g.tile_shift = 0;
     while ((1u << g.tile_shift) < tile) g.tile_shift++;
-    g.small_max = c->cfg.small_tri_pixels ? c->cfg.small_tri_pixels : 64;
-    g.piece = std::max(32u, (g.small_max + 7u) / 8u);  // at most 8 pieces per small triangle
+    g.small_max = c->cfg.small_tri_pixels ? c->cfg.small_tri_pixels : 4096;
     const int w = (int)W, h = (int)W;
     uint32_t base = 0;
     bins.clear();
@@ -662,7 +661,9 @@ int rad_shoot(rad_ctx* c, uint32_t n_shots, rad_stats* stats) {
     return RAD_OK;
 }
 
-int rad_profile_stages(rad_ctx* c, uint32_t n_shots, double* stage_ms, rad_stats* stats) {
+// Stage-by-stage batches with events between stages (rad_profile_stages); `phases` runs the
+// raster kernel that also counts SM cycles per phase (slower; rad_profile_raster_phases).
+static int profile_batches(rad_ctx* c, uint32_t n_shots, double* stage_ms, rad_stats* stats, bool phases) {
     if (!c || !stage_ms) return RAD_E_INVALID;
     if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
     Batch& b = c->shoot.b;
@@ -686,7 +687,7 @@ int rad_profile_stages(rad_ctx* c, uint32_t n_shots, double* stage_ms, rad_stats
         RAD_CUDA(c, cudaEventRecord(ev[3], s));
         launch_bins(c->geo, b, c->d_state, s);
         RAD_CUDA(c, cudaEventRecord(ev[4], s));
-        launch_raster(c->geo, b, c->d_fftab, c->d_state, false, true, s, true);
+        launch_raster(c->geo, b, c->d_fftab, c->d_state, false, true, s, true, phases);
         RAD_CUDA(c, cudaEventRecord(ev[5], s));
         launch_update(c->geo, b, c->d_color, c->d_rho, c->d_area, c->d_rad, c->d_state, s);
         RAD_CUDA(c, cudaEventRecord(ev[6], s));
@@ -714,6 +715,21 @@ int rad_profile_stages(rad_ctx* c, uint32_t n_shots, double* stage_ms, rad_stats
         stats->device_ms = total_ms;
     }
     if (after.overflow) return fail(c, RAD_E_OVERFLOW, "triangle or bin capacity exceeded");
+    return RAD_OK;
+}
+
+int rad_profile_stages(rad_ctx* c, uint32_t n_shots, double* stage_ms, rad_stats* stats) {
+    return profile_batches(c, n_shots, stage_ms, stats, false);
+}
+
+int rad_profile_raster_phases(rad_ctx* c, uint32_t n_shots, uint64_t* cycles, rad_stats* stats) {
+    if (!c || !cycles) return RAD_E_INVALID;
+    double ms[RAD_N_STAGES] = {0};
+    const int rc = profile_batches(c, n_shots, ms, stats, true);
+    if (rc) return rc;
+    unsigned long long ctr[16];
+    RAD_CUDA(c, cudaMemcpy(ctr, c->d_state->raster_counters, sizeof(ctr), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 8; k++) cycles[k] = ctr[8 + k];
     return RAD_OK;
 }
 
@@ -787,7 +803,7 @@ int rad_autotune(rad_ctx* c, uint32_t flags, rad_tuning* out) {
     const uint32_t want = std::max<uint32_t>(8, std::min<uint32_t>(K0, 64));
     for (uint32_t i = 0; sh.size() < want && i < want; i++) sh.push_back((uint32_t)(((uint64_t)i * 2654435761u) % c->n));
     const uint32_t tiles[3] = {16, 32, 64};
-    const uint32_t smalls[7] = {16, 32, 64, 128, 256, 512, 1024};
+    const uint32_t smalls[4] = {64, 256, 1024, 4096};
     uint32_t best_t = 0, best_s = 0, cand = 0;
     float best = 1e30f;
     for (uint32_t t : tiles) {
@@ -1390,8 +1406,7 @@ int rad_set_progress(rad_ctx* c, uint32_t shots_done, double initial_power) {
 int rad_raster_counters(rad_ctx* c, uint64_t* out) {
     if (!c || !out) return RAD_E_INVALID;
     RAD_CUDA(c, cudaStreamSynchronize(c->stream));
-    RAD_CUDA(c, cudaMemcpy(out, c->d_state->raster_counters, sizeof(c->d_state->raster_counters),
-                           cudaMemcpyDeviceToHost));
+    RAD_CUDA(c, cudaMemcpy(out, c->d_state->raster_counters, sizeof(uint64_t) * 8, cudaMemcpyDeviceToHost));
     return RAD_OK;
 }
 

@@ -61,10 +61,8 @@ struct Geo {
     uint32_t nb;               // bins per hemicube
     uint32_t tile;             // bin side
     uint32_t mode;             // rad_mode
-    uint32_t small_max;        // lane-mode threshold (clamped bbox pixels)
-    uint32_t piece;            // box pixels per lane piece of a small triangle, >= small_max / 8
+    uint32_t small_max;        // span-raster threshold (box clamped to a bin, pixels)
     uint32_t tile_shift;       // log2(tile)
-    uint32_t pad0;
     FaceInfo face[5];
     float proj[16];            // Perspective(90,1,0.01,1000), column-major
 };
@@ -82,8 +80,11 @@ struct DevState {
     uint32_t timeouts;
     uint32_t pad[3];
     // raster counters (filled when counting is on): record-bin pairs, small records, small box px,
-    // big records, big stamps in bbox, stamps visited, stamps fully inside, big pixels plotted
-    unsigned long long raster_counters[8];
+    // big records, big stamps in bbox, stamps visited, stamps fully inside, big pixels plotted;
+    // then (phase profiling only) SM cycles summed over warps per raster phase: bin set-up,
+    // record staging, row ownership, row spans, pixel stream, pass barrier, big records and
+    // chunk barrier, bin end
+    unsigned long long raster_counters[16];
 };
 
 // Device pointers of one batch of K hemicubes.
@@ -123,7 +124,7 @@ void launch_setup(const Geo& g, const Batch& b, const float* verts, DevState* st
 void launch_bins(const Geo& g, const Batch& b, DevState* st, cudaStream_t s);
 cudaError_t raster_init();  // per device, before the first launch_raster (dynamic shared memory limits)
 void launch_raster(const Geo& g, const Batch& b, const float* fftab, DevState* st, bool write_items,
-                   bool fused_reduce, cudaStream_t s, bool count = false);
+                   bool fused_reduce, cudaStream_t s, bool count = false, bool phases = false);
 void launch_reduce_items(const Geo& g, const Batch& b, const float* fftab, uint32_t count, cudaStream_t s);
 void launch_fq_to_float(const Geo& g, const Batch& b, uint32_t count, float* out, cudaStream_t s);
 void launch_select(const Geo& g, const Batch& b, const float4* rad, const float* area, DevState* st,

@@ -13,13 +13,14 @@
 //   k_scan     exclusive scan of the bin counts
 //   k_fill     scatters record indices into per-bin lists
 //   k_raster   CTA per (hemicube, tile x tile bin): depth|id keys in shared memory
-//              (atomicMin = GL_LESS with patch-index draw order), small records one
-//              lane each, big triangles one warp each; then either the uint32 item
-//              buffer or the fused reduction: each pixel's delta FF is an exact
-//              multiple of 2^-61, summed per run of equal ids down each column into
-//              a per-bin id -> sum table, flushed with one 64-bit atomicAdd per id
-//              into Fq[hemicube][id].  k_reduce_items does the same for caller item
-//              buffers with __match_any_sync groups and exact redux.sync sums.
+//              (atomicMin = GL_LESS with patch-index draw order).  Small records
+//              (extent <= 64 px) are rasterised by exact integer row spans laid out as
+//              one packed pixel stream per warp; big triangles one warp each in 8x4
+//              stamps.  Then either the uint32 item buffer or the fused reduction:
+//              each pixel's delta FF is an exact multiple of 2^-61, summed per run of
+//              equal ids down each column and added to Fq[hemicube][id] with one 64-bit
+//              atomic per run.  k_reduce_items does the same for caller item buffers
+//              with __match_any_sync groups and exact redux.sync sums.
 // The raster rules are spelled out in oracle/oracle.h (the CPU restatement the
 // parity tests compare against bit for bit).
 #include <cuda_runtime.h>
@@ -681,6 +682,17 @@ __device__ __forceinline__ uint32_t depth_ordinal(float d) {
     return 0x7F800000u - bits;
 }
 
+// ff * 2^61 as an integer, exactly, for a delta form factor ff (an integer multiple of 2^-61
+// below 1; zero for zero): the float's significand shifted by its exponent, with integer
+// instructions only (no 64-bit conversion unit).
+__device__ __forceinline__ unsigned long long ff_fixed61(float ff) {
+    const uint32_t bits = __float_as_uint(ff);
+    if (bits == 0u) return 0ull;
+    const unsigned long long m = (unsigned long long)((bits & 0x7FFFFFu) | 0x800000u);
+    const int sh = (int)(bits >> 23) - 89;  // ff * 2^61 = m * 2^(e - 127 - 23 + 61)
+    return sh >= 0 ? m << sh : m >> -sh;
+}
+
 // Exact warp-segmented sum of q over lanes sharing `key`; returns the group's sum
 // on every lane and the group mask in *gm.
 __device__ __forceinline__ unsigned long long group_sum(unsigned long long key, unsigned long long q, unsigned* gm) {
@@ -692,19 +704,14 @@ __device__ __forceinline__ unsigned long long group_sum(unsigned long long key, 
 }
 
 constexpr int32_t kSmallExtent = 16384;  // 64 px in 24.8 fixed point: edge values fit int32
-constexpr int kChunk = 256;          // triangle records staged per CTA round
-constexpr int kHashSlots = 1024;     // per-bin id -> sum table of the reduction phase
-constexpr uint32_t kHashEmpty = 0xFFFFFFFFu;
-constexpr int kSizeClasses = 16;               // ceil(log2(box pixels)) for boxes <= 2^15 px
-constexpr int kMaxPieces = 8;                  // pieces per small record (g.piece >= small_max / 8)
 
-// The parts of a record the per-pixel loops need (68 bytes in shared memory): the
-// two triangles A = (v0,v1,v2), B = (v0,v2,v3) with their depth planes.
+// A big record's parts the warp path needs (68 bytes in shared memory): the two triangles
+// A = (v0,v1,v2), B = (v0,v2,v3) with their depth planes.
 struct RQuad {
     int32_t X[4], Y[4];
     float c0[2], ax[2], ay[2];
     uint32_t id, flags;  // flags: kRecA | kRecB
-    uint32_t pad;        // 17-word stride: lanes reading different records hit different banks
+    uint32_t pad;
 };
 // One triangle, for the warp path.
 struct RTri {
@@ -712,16 +719,8 @@ struct RTri {
     float c0, ax, ay;
     uint32_t id;
 };
-// one region, two uses: the chunk's records + clamped boxes, then the reduction's hash table
-constexpr int kStageBytes = kChunk * (int)(sizeof(RQuad) + sizeof(short4));
-constexpr int kRegionBytes = kStageBytes > 12 * kHashSlots ? kStageBytes : 12 * kHashSlots;  // 19 KB
-static_assert(kChunk * sizeof(RQuad) % 8 == 0, "clamped boxes follow the records");
-static_assert(kChunk <= 256, "chunk indices are stored as uint8");
-template <int TILE>
-constexpr int raster_dyn_smem() { return TILE * TILE * 8 + kRegionBytes; }
 
 __device__ __forceinline__ bool inside_edge(long long e, bool tl) { return e > 0 || (e == 0 && tl); }
-__device__ __forceinline__ bool inside_edge32(int32_t e, bool tl) { return e > 0 || (e == 0 && tl); }
 
 // Exclusive prefix sum of v over a 256-thread block; returns this thread's offset and
 // leaves the block total in ws[8].  Contains two __syncthreads.
@@ -746,98 +745,6 @@ __device__ __forceinline__ int block_exclusive_scan(int v, uint32_t* ws) {
     }
     __syncthreads();
     return (int)ws[warp] + x - v;
-}
-
-// 64-bit add as two native 32-bit shared atomics: the low word first, its carry into the
-// high word.  Every add commutes, so the final 64-bit value is the exact sum; the table is
-// read only after a barrier.
-__device__ __forceinline__ void shared_add64(unsigned long long* p, unsigned long long v) {
-    uint32_t* w = reinterpret_cast<uint32_t*>(p);  // w[0] = low word, w[1] = high word
-    const uint32_t lo = (uint32_t)v, hi = (uint32_t)(v >> 32);
-    const uint32_t old = atomicAdd(&w[0], lo);
-    const uint32_t up = hi + ((uint32_t)(old + lo) < old ? 1u : 0u);
-    if (up) atomicAdd(&w[1], up);
-}
-
-// Adds an exact partial sum to the bin's open-addressing id -> sum table (linear probing,
-// at most 32 probes); a crowded table sends the sum straight to the global row.
-__device__ __forceinline__ void hash_add(uint32_t* h_id, unsigned long long* h_sum, unsigned long long* Fq,
-                                         uint32_t id, unsigned long long sum) {
-    uint32_t slot = (id * 2654435761u) >> 22;
-    for (int probe = 0; probe < 32; probe++) {
-        uint32_t cur = h_id[slot];
-        if (cur == kHashEmpty) {
-            cur = atomicCAS(&h_id[slot], kHashEmpty, id);
-            if (cur == kHashEmpty) cur = id;
-        }
-        if (cur == id) {
-            shared_add64(&h_sum[slot], sum);
-            return;
-        }
-        slot = (slot + 1) & (kHashSlots - 1);
-    }
-    atomicAdd(&Fq[id], sum);
-}
-
-// One lane rasterises pixels [start, start + steps) of a small record's clamped bbox
-// [x0,x1]x[y0,y1] (row-major flat order) with 32-bit incremental edge functions (exact:
-// |E| < 2^30 for extents <= 64 px), one flat loop of `steps` iterations.  Six edges:
-// A = v0->v1, v1->v2, v2->v0 and B = v0->v2, v2->v3, v3->v0, each with its own
-// top-left flag.  Each is tracked as f = E + tl - 1, so "inside" (E > 0, or E == 0 on
-// a top-left edge) is f >= 0 and a triangle covers the pixel iff the OR of its three
-// f is >= 0; a triangle absent from the record has one f pinned at -1.  B's diagonal
-// v0->v2 is not tracked: its E is exactly -E of A's v2->v0, and exactly one of the two
-// is top-left (a present triangle has v0 != v2: zero-area triangles are culled), so its
-// f is ~f(v2->v0).  A pixel inside both triangles (possible only where a record's
-// snapped outline folds over) takes the smaller key, as two separate draws would.  The
-// record's fields are copied to registers first: the atomics write shared memory, so
-// reads through `t` would be repeated.
-template <int TILE>
-__device__ __forceinline__ void raster_small(const RQuad& t, int x0, int x1, int y0, int start, int steps,
-                                             const BinInfo& bi, int sx, int sy, unsigned long long* key) {
-    const int w = x1 - x0 + 1;
-    const int ry = start / w, rx = start - ry * w;
-    int px = x0 + rx, py = y0 + ry;
-    const float c0a = t.c0[0], axa = t.ax[0], aya = t.ay[0];
-    const float c0b = t.c0[1], axb = t.ax[1], ayb = t.ay[1];
-    const uint32_t id = t.id, flags = t.flags;
-    // f[0..2]: A's edges v0->v1, v1->v2, v2->v0; f[3], f[4]: B's edges v2->v3, v3->v0
-    int32_t f[5], st[5], rs[5];
-#pragma unroll
-    for (int k = 0; k < 5; k++) {
-        const int a = k == 0 ? 0 : (k == 1 ? 1 : (k == 2 ? 2 : (k == 3 ? 2 : 3)));  // from
-        const int j = k == 0 ? 1 : (k == 1 ? 2 : (k == 2 ? 0 : (k == 3 ? 3 : 0)));  // to
-        const int32_t dx = t.X[j] - t.X[a], dy = t.Y[j] - t.Y[a];
-        const bool tl = (t.Y[j] < t.Y[a]) || (t.Y[j] == t.Y[a] && t.X[j] < t.X[a]);
-        f[k] = dx * (py * 256 + 128 - t.Y[a]) - dy * (px * 256 + 128 - t.X[a]) - (tl ? 0 : 1);
-        st[k] = -dy * 256;                  // one pixel right
-        rs[k] = dx * 256 + dy * 256 * (w - 1);  // from (x1, y) to (x0, y + 1)
-    }
-    if (!(flags & kRecA)) f[0] = -1, st[0] = 0, rs[0] = 0;
-    if (!(flags & kRecB)) f[3] = -1, st[3] = 0, rs[3] = 0;
-    int idx = (py - bi.y0) * TILE + (px - bi.x0);
-    const int rowjump = TILE - (w - 1);
-    for (int i = 0; i < steps; i++) {
-        const int32_t ca = f[0] | f[1] | f[2], cb = ~f[2] | f[3] | f[4];
-        if ((ca & cb) >= 0) {
-            // one plane per lane (A when inside A, else B), so the warp evaluates one depth
-            const bool ina = ca >= 0;
-            const float c0 = ina ? c0a : c0b, ax = ina ? axa : axb, ay = ina ? aya : ayb;
-            const float u = (float)(px - sx), wv = (float)(py - sy);
-            unsigned long long k = ((unsigned long long)depth_ordinal((c0 + ax * u) + ay * wv) << 32) | id;
-            if (ina && cb >= 0) {  // inside both (a folded outline): the smaller of the two keys
-                const unsigned long long kb = ((unsigned long long)depth_ordinal((c0b + axb * u) + ayb * wv) << 32) | id;
-                k = kb < k ? kb : k;
-            }
-            atomicMin(&key[idx], k);
-        }
-        const bool wrap = px == x1;
-        px = wrap ? x0 : px + 1;
-        py += wrap ? 1 : 0;
-        idx += wrap ? rowjump : 1;
-#pragma unroll
-        for (int k = 0; k < 5; k++) f[k] += wrap ? rs[k] : st[k];
-    }
 }
 
 // Triangle A (which = 0) or B (which = 1) of a record, for the warp path.
@@ -947,172 +854,68 @@ __device__ __forceinline__ void raster_big(const RTri& t, int x0, int x1, int y0
     if (cnt) atomicAdd(&cnt[7], plotted);
 }
 
+// The big records of a chunk: one warp per triangle of a record (A, then B).  Record i is
+// the RQuad at recs + i * stride bytes.
+// The big records of a chunk: one warp per triangle of a record (A, then B).  Record i is
+// the RQuad at recs + i * stride bytes.
 template <int TILE>
-__global__ void __launch_bounds__(256, 4) k_raster(Geo g, Batch b, const float* __restrict__ fftab, DevState* st,
-                                                   int write_items, int fused, int count) {
-    if (st->stopped) return;
-    const uint32_t gb = blockIdx.x;
-    const uint32_t hi = gb / g.nb, bin = gb % g.nb;
-    const BinInfo bi = b.bins[bin];
-    const bool valid = b.valid[hi] != 0;
-    // dynamic shared memory: the bin's depth|id keys, then one region with two uses: the
-    // chunk's records + clamped boxes during the raster phase, then the per-bin
-    // id -> exact-sum hash table of the reduction phase
-    extern __shared__ __align__(16) unsigned char s_dyn[];
-    unsigned long long* key = reinterpret_cast<unsigned long long*>(s_dyn);
-    unsigned char* s_region = s_dyn + TILE * TILE * 8;
-    RQuad* s_tri = reinterpret_cast<RQuad*>(s_region);
-    short4* s_box = reinterpret_cast<short4*>(s_region + kChunk * sizeof(RQuad));
-    __shared__ uint8_t s_order[kChunk];  // small triangles by size class (ascending)
-    __shared__ uint8_t s_bigi[kChunk];   // big triangles
-    __shared__ uint32_t s_ncls[kSizeClasses];
-    __shared__ uint16_t s_poff[kChunk];                 // first piece of each sorted small triangle
-    __shared__ uint8_t s_owner[kChunk * kMaxPieces];    // piece -> sorted position
-    __shared__ uint32_t s_wsum[9];
-    __shared__ int s_nbig, s_nsmall;
-    __shared__ uint32_t s_cnt[8];
-    uint32_t* ctr = count ? s_cnt : nullptr;
-    if (threadIdx.x < 8) s_cnt[threadIdx.x] = 0;
-    for (int j = threadIdx.x; j < TILE * TILE; j += blockDim.x) key[j] = ~0ull;
-    const int lane = threadIdx.x & 31;
-    __syncthreads();
-    if (valid) {
-        const FaceInfo& F = g.face[bi.face];
-        const int sx = F.sc[0], sy = F.sc[1];
-        uint32_t cnt = b.bin_count[gb], off = b.bin_offset[gb];
-        if (off >= b.list_cap) cnt = 0;
-        else if (off + cnt > b.list_cap) cnt = b.list_cap - off;
-        const int bx1 = bi.x0 + bi.w - 1, by1 = bi.y0 + bi.h - 1;
-        for (uint32_t base = 0; base < cnt; base += kChunk) {
-            const uint32_t m = min((uint32_t)kChunk, cnt - base);
-            if (threadIdx.x < kSizeClasses) s_ncls[threadIdx.x] = 0;
-            if (threadIdx.x == 0) s_nbig = 0;
-            __syncthreads();
-            // 1. load, clamp to the bin, split small (one lane) / big (one warp); small
-            //    triangles are counted per size class ceil(log2(box pixels))
-            int cls = -1;
-            uint32_t rank = 0;
-            if (threadIdx.x < m) {
-                const int4* tr = reinterpret_cast<const int4*>(&b.tris[b.bin_list[off + base + threadIdx.x]]);
-                const int4 xs = tr[0], ys = tr[1], p = tr[2], q = tr[3];  // q = ay[1], id, bx, by
-                const int px0 = q.z & 0xFFF, px1 = (q.z >> 12) & 0xFFF;
-                const int py0 = q.w & 0xFFF, py1 = (q.w >> 12) & 0xFFF;
-                const int x0 = max(px0, (int)bi.x0), x1 = min(px1, bx1);
-                const int y0 = max(py0, (int)bi.y0), y1 = min(py1, by1);
-                if (x0 <= x1 && y0 <= y1) {
-                    RQuad t;
-                    t.X[0] = xs.x; t.X[1] = xs.y; t.X[2] = xs.z; t.X[3] = xs.w;
-                    t.Y[0] = ys.x; t.Y[1] = ys.y; t.Y[2] = ys.z; t.Y[3] = ys.w;
-                    // the planes' constant terms at the scissor origin, rebuilt with the
-                    // set-up's float operations (gx = ax / 256 exactly)
-                    const float d0 = __int_as_float(p.x);
-                    const float ox = (float)((long long)sx * 256 + 128 - xs.x);
-                    const float oy = (float)((long long)sy * 256 + 128 - ys.x);
-                    t.ax[0] = __int_as_float(p.y);
-                    t.ax[1] = __int_as_float(p.z);
-                    t.ay[0] = __int_as_float(p.w);
-                    t.ay[1] = __int_as_float(q.x);
-                    t.c0[0] = (d0 + (t.ax[0] * 0x1p-8f) * ox) + (t.ay[0] * 0x1p-8f) * oy;
-                    t.c0[1] = (d0 + (t.ax[1] * 0x1p-8f) * ox) + (t.ay[1] * 0x1p-8f) * oy;
-                    t.id = (uint32_t)q.y;
-                    t.flags = (uint32_t)q.z & (kRecA | kRecB);
-                    s_tri[threadIdx.x] = t;
-                    const int32_t ex = max(max(t.X[0], t.X[1]), max(t.X[2], t.X[3])) -
-                                       min(min(t.X[0], t.X[1]), min(t.X[2], t.X[3]));
-                    const int32_t ey = max(max(t.Y[0], t.Y[1]), max(t.Y[2], t.Y[3])) -
-                                       min(min(t.Y[0], t.Y[1]), min(t.Y[2], t.Y[3]));
-                    const int area = (x1 - x0 + 1) * (y1 - y0 + 1);
-                    if (ex <= kSmallExtent && ey <= kSmallExtent && area <= (int)g.small_max) {
-                        s_box[threadIdx.x] = make_short4((short)x0, (short)x1, (short)y0, (short)y1);
-                        cls = area > 1 ? 32 - __clz(area - 1) : 0;
-                        rank = atomicAdd(&s_ncls[cls], 1u);
-                        if (ctr) {
-                            atomicAdd(&ctr[1], 1u);
-                            atomicAdd(&ctr[2], (uint32_t)area);
-                        }
-                    } else {
-                        s_bigi[atomicAdd(&s_nbig, 1)] = (uint8_t)threadIdx.x;
-                        if (ctr) atomicAdd(&ctr[3], 1u);
-                    }
-                }
-            }
-            __syncthreads();
-            // 2. class bases (exclusive scan of kSizeClasses counters)
-            if (threadIdx.x == 0) {
-                uint32_t run = 0;
-                for (int k = 0; k < kSizeClasses; k++) {
-                    const uint32_t v = s_ncls[k];
-                    s_ncls[k] = run;
-                    run += v;
-                }
-                s_nsmall = (int)run;
-            }
-            __syncthreads();
-            if (cls >= 0) s_order[s_ncls[cls] + rank] = (uint8_t)threadIdx.x;
-            __syncthreads();
-            // 3. small triangles in size order, each cut into L <= kMaxPieces equal pieces of
-            //    at most g.piece box pixels, one piece per lane: lanes and warps get similar
-            //    amounts of work; then big triangles, one per warp (no barrier between)
-            const int nsmall = s_nsmall, nbig = s_nbig;
-            int np = 0;
-            if ((int)threadIdx.x < nsmall) {
-                const short4 bx = s_box[s_order[threadIdx.x]];
-                const int area = (bx.y - bx.x + 1) * (bx.w - bx.z + 1);
-                np = (area + (int)g.piece - 1) / (int)g.piece;
-            }
-            const int poff = block_exclusive_scan(np, s_wsum);  // syncs; s_wsum[8] = total
-            if (np) {
-                s_poff[threadIdx.x] = (uint16_t)poff;
-                for (int j = 0; j < np; j++) s_owner[poff + j] = (uint8_t)threadIdx.x;
-            }
-            __syncthreads();
-            const int npieces = (int)s_wsum[8];
-            for (int gp = threadIdx.x; gp < npieces; gp += blockDim.x) {
-                const int pos = s_owner[gp], i = s_order[pos];
-                const short4 bx = s_box[i];
-                const int w = bx.y - bx.x + 1, area = w * (bx.w - bx.z + 1);
-                const int L = (area + (int)g.piece - 1) / (int)g.piece, per = (area + L - 1) / L;
-                const int start = (gp - (int)s_poff[pos]) * per;
-                raster_small<TILE>(s_tri[i], bx.x, bx.y, bx.z, start, min(per, area - start), bi, sx, sy, key);
-            }
-            // big records: one warp per triangle of the record (A, then B)
-            for (int i = (int)(threadIdx.x >> 5); i < 2 * nbig; i += (int)(blockDim.x >> 5)) {
-                const RQuad& q = s_tri[s_bigi[i >> 1]];
-                const int which = i & 1;
-                if (!(q.flags & (which ? kRecB : kRecA))) continue;
-                const RTri t = rec_tri(q, which);
-                const int32_t xmn = min(t.X[0], min(t.X[1], t.X[2])), xmx = max(t.X[0], max(t.X[1], t.X[2]));
-                const int32_t ymn = min(t.Y[0], min(t.Y[1], t.Y[2])), ymx = max(t.Y[0], max(t.Y[1], t.Y[2]));
-                const int x0 = max((int)floordiv256((long long)xmn - 128 + 255), (int)bi.x0);
-                const int x1 = min((int)floordiv256((long long)xmx - 128), bx1);
-                const int y0 = max((int)floordiv256((long long)ymn - 128 + 255), (int)bi.y0);
-                const int y1 = min((int)floordiv256((long long)ymx - 128), by1);
-                if (x0 <= x1 && y0 <= y1) raster_big<TILE>(t, x0, x1, y0, y1, bi, sx, sy, key, lane, ctr);
-            }
-            __syncthreads();
-        }
+__device__ __forceinline__ void raster_big_records(const unsigned char* recs, int stride, const uint8_t* bigi,
+                                                   int nbig, const BinInfo& bi, int sx, int sy,
+                                                   unsigned long long* key, int lane, uint32_t* ctr) {
+    const int bx1 = bi.x0 + bi.w - 1, by1 = bi.y0 + bi.h - 1;
+    for (int i = (int)(threadIdx.x >> 5); i < 2 * nbig; i += (int)(blockDim.x >> 5)) {
+        const RQuad& q = *reinterpret_cast<const RQuad*>(recs + (size_t)bigi[i >> 1] * stride);
+        const int which = i & 1;
+        if (!(q.flags & (which ? kRecB : kRecA))) continue;
+        const RTri t = rec_tri(q, which);
+        const int32_t xmn = min(t.X[0], min(t.X[1], t.X[2])), xmx = max(t.X[0], max(t.X[1], t.X[2]));
+        const int32_t ymn = min(t.Y[0], min(t.Y[1], t.Y[2])), ymx = max(t.Y[0], max(t.Y[1], t.Y[2]));
+        const int x0 = max((int)floordiv256((long long)xmn - 128 + 255), (int)bi.x0);
+        const int x1 = min((int)floordiv256((long long)xmx - 128), bx1);
+        const int y0 = max((int)floordiv256((long long)ymn - 128 + 255), (int)bi.y0);
+        const int y1 = min((int)floordiv256((long long)ymx - 128), by1);
+        if (x0 <= x1 && y0 <= y1) raster_big<TILE>(t, x0, x1, y0, y1, bi, sx, sy, key, lane, ctr);
     }
-    // The reduction's delta form factors are loaded now, ahead of the barrier, so that
-    // their L2 latency overlaps the barrier and the hash-table clear (kSeg per thread,
-    // the column segment the thread walks below).
-    constexpr int kSeg = TILE * TILE / 256 > 4 ? TILE * TILE / 256 : 4;
-    constexpr int kWalkers = TILE * TILE / kSeg;
+}
+
+// The end of a bin, after its records are rasterised (all threads): the counters, the item
+// buffer (write_items) and the fused reduction (fused).  For the reduction each thread walks
+// kSeg pixels down one column of the bin, summing the exact fixed-point delta form factors
+// (ff * 2^61, integers) while the patch id stays the same, and adds each run's sum to the
+// hemicube's row with one 64-bit atomic.  Integer sums commute, so the row is exact and
+// independent of the order of the adds.  Lanes take adjacent columns (conflict-free key
+// reads, coalesced table reads).
+template <int TILE>
+__host__ __device__ constexpr int finish_seg() { return TILE * TILE / 256 > 4 ? TILE * TILE / 256 : 4; }  // pixels per walker
+
+// The walker's column segment of the bin's delta form factors (an L2-resident table).
+template <int TILE>
+__device__ __forceinline__ void finish_load(const Geo& g, const float* __restrict__ fftab, const BinInfo& bi,
+                                            bool walker, float* ffv) {
+    constexpr int kSeg = finish_seg<TILE>();
     const int wx = threadIdx.x % TILE, wr0 = (threadIdx.x / TILE) * kSeg;
-    const bool walker = fused && valid && (int)threadIdx.x < kWalkers;
-    float ffv[kSeg];
 #pragma unroll
     for (int i = 0; i < kSeg; i++) {
         ffv[i] = 0.f;
         if (walker && wx < bi.w && wr0 + i < bi.h) ffv[i] = fftab[(size_t)(bi.y0 + wr0 + i) * g.TW + bi.x0 + wx];
     }
-    __syncthreads();
+}
+
+// Called after a barrier that follows the bin's last key update (all threads).
+template <int TILE>
+__device__ __forceinline__ void raster_finish(const Geo& g, const Batch& b, DevState* st, int write_items,
+                                              int count, uint32_t gb, uint32_t hi, const BinInfo& bi, bool valid,
+                                              bool walker, const float* ffv, const unsigned long long* key,
+                                              const uint32_t* s_cnt) {
+    constexpr int kSeg = finish_seg<TILE>();
+    const int wx = threadIdx.x % TILE, wr0 = (threadIdx.x / TILE) * kSeg;
     if (count && threadIdx.x < 8) {
         uint32_t v = s_cnt[threadIdx.x];
         if (threadIdx.x == 0) v = valid ? min(b.bin_count[gb], b.list_cap) : 0u;
         if (v) atomicAdd(&st->raster_counters[threadIdx.x], (unsigned long long)v);
     }
-    const size_t img = (size_t)hi * g.RES;
-    if (write_items)
+    if (write_items) {
+        const size_t img = (size_t)hi * g.RES;
         for (int j = threadIdx.x; j < TILE * TILE; j += blockDim.x) {
             const int ly = j / TILE, lx = j % TILE;
             if (lx >= bi.w || ly >= bi.h) continue;
@@ -1120,75 +923,375 @@ __global__ void __launch_bounds__(256, 4) k_raster(Geo g, Batch b, const float* 
             const bool has = valid && k != ~0ull;
             b.items[img + (size_t)(bi.y0 + ly) * g.TW + bi.x0 + lx] = has ? (uint32_t)k + 1u : 0u;
         }
-    if (!fused) return;
-    uint32_t* h_id = reinterpret_cast<uint32_t*>(s_region);
-    unsigned long long* h_sum = reinterpret_cast<unsigned long long*>(s_region + 4 * kHashSlots);
-    for (int j = threadIdx.x; j < kHashSlots; j += blockDim.x) {
-        h_id[j] = kHashEmpty;
-        h_sum[j] = 0;
     }
-    __syncthreads();
+    if (!walker) return;
     unsigned long long* Fq = b.Fq + (size_t)hi * g.n;
-    // Each thread walks kSeg consecutive pixels down one column of the bin, summing the
-    // exact fixed-point delta form factors (ff * 2^61) while the patch id stays the same,
-    // and adds each run's sum to the bin's id -> sum table once.  Lanes take adjacent
-    // columns, so key reads are conflict-free.
-    if (walker) {
-        const bool col_in = wx < bi.w;
-        uint32_t cur = kHashEmpty;
-        unsigned long long acc = 0;
+    const bool col_in = wx < bi.w;
+    uint32_t cur = 0xFFFFFFFFu;
+    unsigned long long acc = 0;
 #pragma unroll
-        for (int i = 0; i < kSeg; i++) {
-            const unsigned long long k = key[(wr0 + i) * TILE + wx];
-            const bool has = col_in && wr0 + i < bi.h && k != ~0ull;
-            const uint32_t id = has ? (uint32_t)k : kHashEmpty;
-            if (id != cur) {
-                if (cur != kHashEmpty) hash_add(h_id, h_sum, Fq, cur, acc);
-                cur = id;
-                acc = 0;
-            }
-            if (has) acc += __float2ull_rz(ffv[i] * 0x1p61f);
+    for (int i = 0; i < kSeg; i++) {
+        const unsigned long long k = key[(wr0 + i) * TILE + wx];
+        const bool has = col_in && wr0 + i < bi.h && k != ~0ull;
+        const uint32_t id = has ? (uint32_t)k : 0xFFFFFFFFu;
+        if (id != cur) {
+            if (cur != 0xFFFFFFFFu) atomicAdd(&Fq[cur], acc);
+            cur = id;
+            acc = 0;
         }
-        if (cur != kHashEmpty) hash_add(h_id, h_sum, Fq, cur, acc);
+        if (has) acc += ff_fixed61(ffv[i]);
     }
+    if (cur != 0xFFFFFFFFu) atomicAdd(&Fq[cur], acc);
+}
+
+// Small records: exact row spans, then one packed pixel stream per warp.
+//
+// A small record (extent <= 64 px and box clamped to the bin <= small_max px) is staged as the
+// constants of its five tracked edges at the centre of the top-left pixel of its clamped box,
+// so that any row's covered columns follow exactly from integer bounds:
+//   f_e(n, r) = f0_e + r * (dx_e * 256) - n * (dy_e * 256)   (column n, row r of the box)
+// is the biased edge value E + tl - 1 (E the exact 24.8 edge function, tl the top-left flag;
+// inside: f >= 0), and f_e >= 0  <=>  n >= -floor(f_e(0, r) / a_e) when dy_e < 0, or
+// n <= floor(f_e(0, r) / a_e) when dy_e > 0, with a_e = |dy_e| * 256; a horizontal edge
+// (dy_e = 0) admits the whole row or none of it.  Triangle A is edges 0, 1, 2 (v0->v1,
+// v1->v2, v2->v0); B is v0->v2, 3 and 4 (v2->v3, v3->v0), where v0->v2 is the complement of
+// edge 2 (f = -f_2 - 1, so floor(f / a) = -floor(f_2 / a) - 1).  A pixel inside both (a
+// folded outline) is in both spans and gets both keys, the smaller winning, as two draws would.
+struct SpanRec {
+    int32_t f0[5];   // biased edge values at the centre of the box's top-left pixel
+    uint32_t dxy[5]; // (uint16) dx | dy << 16, 24.8 edge vector (|dx|, |dy| <= 16384)
+    float pl[6];     // c0, ax, ay of A, then of B (constant at the scissor origin; gradients x256)
+    uint32_t id;
+    uint32_t geo;    // x0 - bin x0 | (w - 1) << 6 | y0 - bin y0 << 12 | A << 18 | B << 19
+};
+static_assert(sizeof(SpanRec) == 72 && sizeof(RQuad) <= sizeof(SpanRec), "staging slot");
+constexpr int kSpanChunk = 256;    // records staged per CTA round (indices stored as uint8)
+constexpr int kRowCap = 2048;      // rows per pass over a chunk's small records
+constexpr int kRegionBytes = kSpanChunk * (int)sizeof(SpanRec);
+template <int TILE>
+constexpr int raster_dyn_smem() { return TILE * TILE * 8 + kRegionBytes; }
+
+// rcp.approx: relative error about 2^-23, which the exact integer step of floor_div absorbs.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// floor(f / a) for a > 0 (a multiple of 256, at most 2^22) where only results in [-65, 65]
+// matter exactly: a float estimate (relative error a few 2^-24, so off by at most one inside
+// the clamp), clamped, then one exact integer correction.  Outside the clamp the result keeps
+// the right side of [-65, 65], which is all the span bounds need.
+__device__ __forceinline__ int32_t floor_div(int32_t f, int32_t a) {
+    const float q = __int2float_rn(f) * rcp_approx(__int2float_rn(a));
+    int32_t m = max(-66, min(66, __float2int_rd(q)));
+    const int32_t r = f - m * a;  // in [0, a) exactly when m is the floor
+    return m + (r >= a ? 1 : 0) - (r < 0 ? 1 : 0);
+}
+
+// The bound one edge puts on its triangle's span [lo, hi] in a row; lo starts at 0 and hi at
+// w - 1 <= 63, so 0 and 64 are neutral.
+__device__ __forceinline__ void edge_bound(int32_t f, int32_t dy, int& lo, int& hi) {
+    const int32_t m = floor_div(f, max(abs(dy) * 256, 256));
+    lo = max(lo, dy < 0 ? -m : 0);
+    hi = min(hi, dy > 0 ? m : ((dy == 0 && f < 0) ? -1 : 64));
+}
+
+// CTA per (hemicube, TILE x TILE bin), 256 threads, records in chunks of kSpanChunk:
+//  1. each thread stages one record: a small one as a SpanRec, a big one as an RQuad;
+//  2. a block scan numbers the small records' rows, and row items are mapped to records;
+//  3. warps take 32 rows at a time from a shared cursor: each lane computes its row's spans
+//     of A and B, the warp lays the spans' pixels out as one stream, and each lane then takes
+//     one pixel of every 32 (it finds its span through a bit mask of span starts), evaluates
+//     the depth plane and does a 64-bit atomicMin of depth|id into the bin's keys;
+//  4. big records (extent > 64 px or a box above small_max), one warp per triangle;
+// then raster_finish.  PROF adds SM-cycle counters per phase (raster counters 8..15); it is
+// launched only for phase profiling.
+template <int TILE, bool PROF>
+__global__ void __launch_bounds__(256, 4) k_raster(Geo g, Batch b, const float* __restrict__ fftab,
+                                                   DevState* st, int write_items, int fused, int count) {
+    if (st->stopped) return;
+    __shared__ unsigned long long s_cyc[8];
+    long long tmark = PROF ? clock64() : 0;
+    auto mark = [&](int ph) {
+        if (PROF) {
+            const long long t = clock64();
+            if ((threadIdx.x & 31) == 0) atomicAdd(&s_cyc[ph], (unsigned long long)(t - tmark));
+            tmark = t;
+        }
+    };
+    if (PROF && threadIdx.x < 8) s_cyc[threadIdx.x] = 0;
+    const uint32_t gb = blockIdx.x;
+    const uint32_t hi = gb / g.nb, bin = gb % g.nb;
+    const BinInfo bi = b.bins[bin];
+    const bool valid = b.valid[hi] != 0;
+    // dynamic shared memory: the bin's depth|id keys, then the chunk's staged records
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    unsigned long long* key = reinterpret_cast<unsigned long long*>(s_dyn);
+    unsigned char* s_region = s_dyn + TILE * TILE * 8;
+    SpanRec* s_rec = reinterpret_cast<SpanRec*>(s_region);
+    __shared__ uint8_t s_bigi[kSpanChunk];       // big records of the chunk
+    __shared__ uint16_t s_rowbase[kSpanChunk];   // first row item of each small record
+    __shared__ uint8_t s_rowown[kRowCap];        // row item -> record (this pass)
+    __shared__ uint32_t s_seg[8][64];            // per warp: the spans of its 32 rows, in stream order
+    __shared__ uint32_t s_wsum[9];
+    __shared__ int s_nbig;
+    __shared__ int s_next;                       // next unclaimed block of 32 rows
+    __shared__ uint32_t s_cnt[8];
+    uint32_t* ctr = count ? s_cnt : nullptr;
+    if (threadIdx.x < 8) s_cnt[threadIdx.x] = 0;
+    if (threadIdx.x == 0) s_next = 8 * 32;
+    uint32_t cnt = 0, off = 0;
+    if (valid) {
+        cnt = b.bin_count[gb];
+        off = b.bin_offset[gb];
+        if (off >= b.list_cap) cnt = 0;
+        else if (off + cnt > b.list_cap) cnt = b.list_cap - off;
+    }
+    // the first chunk's records are requested before the keys are cleared, so that their
+    // DRAM latency overlaps the clear
+    const bool pre = threadIdx.x < min(cnt, (uint32_t)kSpanChunk);
+    int4 pr0 = make_int4(0, 0, 0, 0), pr1 = pr0, pr2 = pr0, pr3 = pr0;
+    if (pre) {
+        const int4* tr = reinterpret_cast<const int4*>(&b.tris[b.bin_list[off + threadIdx.x]]);
+        pr0 = tr[0];
+        pr1 = tr[1];
+        pr2 = tr[2];
+        pr3 = tr[3];
+    }
+    for (int j = threadIdx.x; j < TILE * TILE; j += blockDim.x) key[j] = ~0ull;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u, le = lt | (1u << lane);
     __syncthreads();
-    for (int j = threadIdx.x; j < kHashSlots; j += blockDim.x) {
-        const uint32_t id = h_id[j];
-        if (id != kHashEmpty) atomicAdd(&Fq[id], h_sum[j]);
+    mark(0);
+    const bool walker = fused && valid && (int)threadIdx.x < TILE * TILE / finish_seg<TILE>();
+    if (valid) {
+        const FaceInfo& F = g.face[bi.face];
+        const int sx = F.sc[0], sy = F.sc[1];
+        const int ux = bi.x0 - sx, uy = bi.y0 - sy;  // bin origin relative to the scissor origin
+        const int bx1 = bi.x0 + bi.w - 1, by1 = bi.y0 + bi.h - 1;
+        for (uint32_t base = 0; base < cnt; base += kSpanChunk) {
+            const uint32_t m = min((uint32_t)kSpanChunk, cnt - base);
+            if (threadIdx.x == 0) s_nbig = 0;
+            __syncthreads();
+            // 1. load, clamp to the bin, stage: small records as SpanRec, big ones as RQuad
+            int rows = 0;
+            if (threadIdx.x < m) {
+                int4 xs = pr0, ys = pr1, p = pr2, q = pr3;  // q = ay[1], id, bx, by
+                if (base != 0) {
+                    const int4* tr = reinterpret_cast<const int4*>(&b.tris[b.bin_list[off + base + threadIdx.x]]);
+                    xs = tr[0];
+                    ys = tr[1];
+                    p = tr[2];
+                    q = tr[3];
+                }
+                const int px0 = q.z & 0xFFF, px1 = (q.z >> 12) & 0xFFF;
+                const int py0 = q.w & 0xFFF, py1 = (q.w >> 12) & 0xFFF;
+                const int x0 = max(px0, (int)bi.x0), x1 = min(px1, bx1);
+                const int y0 = max(py0, (int)bi.y0), y1 = min(py1, by1);
+                if (x0 <= x1 && y0 <= y1) {
+                    const int32_t X[4] = {xs.x, xs.y, xs.z, xs.w}, Y[4] = {ys.x, ys.y, ys.z, ys.w};
+                    // the planes' constant terms at the scissor origin, rebuilt with the
+                    // set-up's float operations (gx = ax / 256 exactly)
+                    const float d0 = __int_as_float(p.x);
+                    const float ox = (float)((long long)sx * 256 + 128 - xs.x);
+                    const float oy = (float)((long long)sy * 256 + 128 - ys.x);
+                    const float axA = __int_as_float(p.y), axB = __int_as_float(p.z);
+                    const float ayA = __int_as_float(p.w), ayB = __int_as_float(q.x);
+                    const float c0A = (d0 + (axA * 0x1p-8f) * ox) + (ayA * 0x1p-8f) * oy;
+                    const float c0B = (d0 + (axB * 0x1p-8f) * ox) + (ayB * 0x1p-8f) * oy;
+                    const uint32_t flags = (uint32_t)q.z & (kRecA | kRecB);
+                    const int32_t ex = max(max(X[0], X[1]), max(X[2], X[3])) - min(min(X[0], X[1]), min(X[2], X[3]));
+                    const int32_t ey = max(max(Y[0], Y[1]), max(Y[2], Y[3])) - min(min(Y[0], Y[1]), min(Y[2], Y[3]));
+                    const int area = (x1 - x0 + 1) * (y1 - y0 + 1);
+                    if (ex <= kSmallExtent && ey <= kSmallExtent && area <= (int)g.small_max) {
+                        SpanRec& r = s_rec[threadIdx.x];
+#pragma unroll
+                        for (int k = 0; k < 5; k++) {
+                            const int a = k == 0 ? 0 : (k == 1 ? 1 : (k == 2 ? 2 : (k == 3 ? 2 : 3)));  // from
+                            const int j = k == 0 ? 1 : (k == 1 ? 2 : (k == 2 ? 0 : (k == 3 ? 3 : 0)));  // to
+                            const int32_t dx = X[j] - X[a], dy = Y[j] - Y[a];
+                            const bool tl = (Y[j] < Y[a]) || (Y[j] == Y[a] && X[j] < X[a]);
+                            r.f0[k] = dx * (y0 * 256 + 128 - Y[a]) - dy * (x0 * 256 + 128 - X[a]) - (tl ? 0 : 1);
+                            r.dxy[k] = ((uint32_t)dx & 0xFFFFu) | ((uint32_t)dy << 16);
+                        }
+                        r.pl[0] = c0A; r.pl[1] = axA; r.pl[2] = ayA;
+                        r.pl[3] = c0B; r.pl[4] = axB; r.pl[5] = ayB;
+                        r.id = (uint32_t)q.y;
+                        r.geo = (uint32_t)(x0 - bi.x0) | ((uint32_t)(x1 - x0) << 6) | ((uint32_t)(y0 - bi.y0) << 12) |
+                                ((flags & kRecA) ? 1u << 18 : 0u) | ((flags & kRecB) ? 1u << 19 : 0u);
+                        rows = y1 - y0 + 1;
+                        if (ctr) {
+                            atomicAdd(&ctr[1], 1u);
+                            atomicAdd(&ctr[2], (uint32_t)area);
+                        }
+                    } else {
+                        RQuad& t = *reinterpret_cast<RQuad*>(&s_rec[threadIdx.x]);
+#pragma unroll
+                        for (int k = 0; k < 4; k++) t.X[k] = X[k], t.Y[k] = Y[k];
+                        t.c0[0] = c0A; t.c0[1] = c0B;
+                        t.ax[0] = axA; t.ax[1] = axB;
+                        t.ay[0] = ayA; t.ay[1] = ayB;
+                        t.id = (uint32_t)q.y;
+                        t.flags = flags;
+                        s_bigi[atomicAdd(&s_nbig, 1)] = (uint8_t)threadIdx.x;
+                        if (ctr) atomicAdd(&ctr[3], 1u);
+                    }
+                }
+            }
+            // 2. row items: record t owns rows [rowbase, rowbase + rows) of the chunk
+            const int rowbase = block_exclusive_scan(rows, s_wsum);  // syncs; s_wsum[8] = total
+            const int nrows = (int)s_wsum[8];
+            mark(1);
+            if (rows) s_rowbase[threadIdx.x] = (uint16_t)rowbase;
+            for (int pass = 0; pass < nrows; pass += kRowCap) {
+                const int np = min(kRowCap, nrows - pass);
+                {
+                    const int r0 = max(rowbase, pass), r1 = min(rowbase + rows, pass + np);
+                    for (int i = r0; i < r1; i++) s_rowown[i - pass] = (uint8_t)threadIdx.x;
+                }
+                __syncthreads();
+                mark(2);
+                // 3. blocks of 32 rows: spans of A and B, then their pixels as one stream
+                uint32_t* seg = s_seg[warp];
+                for (int rb = warp * 32; rb < np;) {  // warp-uniform
+                    const int i = rb + lane;
+                    int lenA = 0, lenB = 0, loA = 0, loB = 0, yl = 0, xl0 = 0, k = 0;
+                    if (i < np) {
+                        k = s_rowown[i];
+                        const SpanRec& R = s_rec[k];
+                        const int r = pass + i - (int)s_rowbase[k];
+                        const uint32_t geo = R.geo;
+                        xl0 = (int)(geo & 63u);
+                        const int w = (int)((geo >> 6) & 63u) + 1;
+                        yl = (int)((geo >> 12) & 63u) + r;
+                        int32_t f[5], dy[5];
+#pragma unroll
+                        for (int e = 0; e < 5; e++) {
+                            const uint32_t d = R.dxy[e];
+                            const int32_t dx = (int32_t)(int16_t)(d & 0xFFFFu);
+                            dy[e] = (int32_t)(int16_t)(d >> 16);
+                            f[e] = R.f0[e] + r * (dx * 256);
+                        }
+                        int hiA = w - 1, hiB = w - 1;
+                        edge_bound(f[0], dy[0], loA, hiA);
+                        edge_bound(f[1], dy[1], loA, hiA);
+                        edge_bound(f[3], dy[3], loB, hiB);
+                        edge_bound(f[4], dy[4], loB, hiB);
+                        // edge 2 bounds A; its complement v0->v2 bounds B
+                        const int32_t m2 = floor_div(f[2], max(abs(dy[2]) * 256, 256));
+                        loA = max(loA, dy[2] < 0 ? -m2 : 0);
+                        hiA = min(hiA, dy[2] > 0 ? m2 : ((dy[2] == 0 && f[2] < 0) ? -1 : 64));
+                        loB = max(loB, dy[2] > 0 ? m2 + 1 : 0);
+                        hiB = min(hiB, dy[2] < 0 ? -m2 - 1 : ((dy[2] == 0 && f[2] >= 0) ? -1 : 64));
+                        if (geo & (1u << 18)) lenA = max(0, hiA - loA + 1);
+                        if (geo & (1u << 19)) lenB = max(0, hiB - loB + 1);
+                    }
+                    // stream offsets of this lane's pixels (warp exclusive scan)
+                    const int n = lenA + lenB;
+                    int x = n;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int y = __shfl_up_sync(0xffffffffu, x, o);
+                        if (lane >= o) x += y;
+                    }
+                    const int total = __shfl_sync(0xffffffffu, x, 31);
+                    const int sA = x - n, sB = sA + lenA;
+                    // span table in stream order: rank = non-empty spans of the lower lanes;
+                    // entry: (start - first column + 64) | row << 13 | triangle << 19 | record << 20
+                    const unsigned bA = __ballot_sync(0xffffffffu, lenA > 0), bB = __ballot_sync(0xffffffffu, lenB > 0);
+                    const int rank = __popc(bA & lt) + __popc(bB & lt);
+                    if (lenA > 0) seg[rank] = (uint32_t)(sA - (xl0 + loA) + 64) | ((uint32_t)yl << 13) | ((uint32_t)k << 20);
+                    if (lenB > 0)
+                        seg[rank + (lenA > 0)] =
+                            (uint32_t)(sB - (xl0 + loB) + 64) | ((uint32_t)yl << 13) | (1u << 19) | ((uint32_t)k << 20);
+                    __syncwarp();
+                    mark(3);
+                    int S = 0;  // spans that start before the window
+                    for (int w0 = 0; w0 < total; w0 += 32) {
+                        uint32_t bits = 0;
+                        if (lenA > 0 && (unsigned)(sA - w0) < 32u) bits |= 1u << (sA - w0);
+                        if (lenB > 0 && (unsigned)(sB - w0) < 32u) bits |= 1u << (sB - w0);
+                        const unsigned starts = __reduce_or_sync(0xffffffffu, bits);
+                        const int gpos = w0 + lane;
+                        if (gpos < total) {
+                            const uint32_t e = seg[S + __popc(starts & le) - 1];
+                            const int xl = gpos - ((int)(e & 0x1FFFu) - 64);
+                            const int ylf = (int)((e >> 13) & 63u);
+                            const SpanRec& R = s_rec[e >> 20];
+                            const float* pl = R.pl + 3 * ((e >> 19) & 1u);
+                            const float u = (float)(ux + xl), wv = (float)(uy + ylf);
+                            const float D = (pl[0] + pl[1] * u) + pl[2] * wv;
+                            atomicMin(&key[ylf * TILE + xl], ((unsigned long long)depth_ordinal(D) << 32) | R.id);
+                        }
+                        S += __popc(starts);
+                    }
+                    __syncwarp();
+                    mark(4);
+                    if (lane == 0) rb = atomicAdd(&s_next, 32);
+                    rb = __shfl_sync(0xffffffffu, rb, 0);
+                }
+                // after the last pass of the last chunk the warps go straight on to the big
+                // records (the chunk barrier below orders them before the bin end)
+                if (!(pass + np >= nrows && base + kSpanChunk >= cnt)) {
+                    __syncthreads();
+                    if (threadIdx.x == 0) s_next = 8 * 32;
+                }
+                mark(5);
+            }
+            // 4. big records: one warp per triangle
+            raster_big_records<TILE>(s_region, (int)sizeof(SpanRec), s_bigi, s_nbig, bi, sx, sy, key, lane, ctr);
+            __syncthreads();
+            mark(6);
+        }
+    }
+    // the walkers' delta form factors (loading them any earlier keeps 16 registers live through
+    // the big-record path, whose 64-bit edge arithmetic then spills)
+    float ffv[finish_seg<TILE>()];
+    finish_load<TILE>(g, fftab, bi, walker, ffv);
+    raster_finish<TILE>(g, b, st, write_items, count, gb, hi, bi, valid, walker, ffv, key, s_cnt);
+    if (PROF) {
+        mark(7);
+        __syncthreads();
+        if (threadIdx.x < 8) atomicAdd(&st->raster_counters[8 + threadIdx.x], s_cyc[threadIdx.x]);
     }
 }
 
-template <int TILE>
+template <int TILE, bool PROF>
 static cudaError_t raster_attrs() {
-    cudaError_t e = cudaFuncSetAttribute(k_raster<TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_raster<TILE, PROF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          raster_dyn_smem<TILE>());
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_raster<TILE>, cudaFuncAttributePreferredSharedMemoryCarveout,
+        e = cudaFuncSetAttribute(k_raster<TILE, PROF>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cudaSharedmemCarveoutMaxShared);
     return e;
 }
 
 cudaError_t raster_init() {
-    cudaError_t e = raster_attrs<16>();
-    if (e == cudaSuccess) e = raster_attrs<32>();
-    if (e == cudaSuccess) e = raster_attrs<64>();
+    cudaError_t e = raster_attrs<16, false>();
+    if (e == cudaSuccess) e = raster_attrs<32, false>();
+    if (e == cudaSuccess) e = raster_attrs<64, false>();
+    if (e == cudaSuccess) e = raster_attrs<16, true>();
+    if (e == cudaSuccess) e = raster_attrs<32, true>();
+    if (e == cudaSuccess) e = raster_attrs<64, true>();
     return e;
 }
 
 void launch_raster(const Geo& g, const Batch& b, const float* fftab, DevState* st, bool write_items,
-                   bool fused_reduce, cudaStream_t s, bool count) {
+                   bool fused_reduce, cudaStream_t s, bool count, bool phases) {
     dim3 grid(b.K * g.nb);
-    switch (g.tile) {
-        case 16:
-            k_raster<16><<<grid, 256, raster_dyn_smem<16>(), s>>>(g, b, fftab, st, write_items, fused_reduce, count);
-            break;
-        case 64:
-            k_raster<64><<<grid, 256, raster_dyn_smem<64>(), s>>>(g, b, fftab, st, write_items, fused_reduce, count);
-            break;
-        default:
-            k_raster<32><<<grid, 256, raster_dyn_smem<32>(), s>>>(g, b, fftab, st, write_items, fused_reduce, count);
-            break;
+#define RAD_RASTER_LAUNCH(T, P) \
+    k_raster<T, P><<<grid, 256, raster_dyn_smem<T>(), s>>>(g, b, fftab, st, write_items, fused_reduce, count)
+    if (phases) {
+        if (g.tile == 16) RAD_RASTER_LAUNCH(16, true);
+        else if (g.tile == 64) RAD_RASTER_LAUNCH(64, true);
+        else RAD_RASTER_LAUNCH(32, true);
+    } else {
+        if (g.tile == 16) RAD_RASTER_LAUNCH(16, false);
+        else if (g.tile == 64) RAD_RASTER_LAUNCH(64, false);
+        else RAD_RASTER_LAUNCH(32, false);
     }
+#undef RAD_RASTER_LAUNCH
 }
 
 // Reduction of caller-provided item buffers (count stacked 2W x 1.5W images).
@@ -1200,7 +1303,7 @@ __global__ void k_reduce_items(Geo g, Batch b, const float* __restrict__ fftab, 
     const bool has = it != 0 && it <= g.n;
     const uint32_t hi = (uint32_t)(idx / g.RES), pix = (uint32_t)(idx % g.RES);
     unsigned long long q = 0;
-    if (has) q = __float2ull_rz(fftab[pix] * 0x1p61f);
+    if (has) q = ff_fixed61(fftab[pix]);
     // the lanes of one warp may span several images (an image is 3W^2 texels: 12 at W = 2),
     // so the key carries the whole image index beside the patch id
     const unsigned long long key = has ? ((unsigned long long)hi << 32) | (it - 1) : ~0ull;

@@ -2,12 +2,12 @@
 
 * The large plain configuration: the seeded 20 x 20 x 5 m room with 40 boxes and 4 ceiling
   emitters (50,538 patches, seed 0), hemicube side 512, K = 128 shooters per batch, PHYS
-  rule, raster bins of 64 px with the 256-px lane/warp split (the configuration the
-  autotuner picks for it and the one the benchmark times).
+  rule, raster bins of 64 px with every record of extent <= 64 px on the span path (the
+  configuration the autotuner picks for it and the one the benchmark times).
   - item buffers of four shooters (a light, a box face, a floor patch, a wall patch),
     bit-exact;
   - fused form-factor rows of the same shooters, bit-exact against the oracle's exact sums
-    of its own item buffers, at two raster configurations;
+    of its own item buffers, at three raster configurations;
   - two K = 128 shoot batches, bit-exact state and the same FP64 residual.
 * The small plain configuration: the reference scene (ModelContainer::load at area 0.045,
   5,171 patches), hemicube side 256, K = 10, REF rule, 20 shots: bit-exact against the
@@ -58,7 +58,7 @@ def test_room50k_sizes(room50k):
 
 def test_room50k_item_buffers_bit_exact(lib, orc, room50k):
     sh = _four_shooters(room50k)
-    with _solver(lib, room50k, 512, 4, 1, tile=64, small_tri_pixels=256) as s:
+    with _solver(lib, room50k, 512, 4, 1, tile=64, small_tri_pixels=4096) as s:
         items = s.item_buffers(sh).reshape(len(sh), -1)
     for k, p in enumerate(sh):
         ref = orc.render(512, room50k["vertices"], int(p))
@@ -66,7 +66,7 @@ def test_room50k_item_buffers_bit_exact(lib, orc, room50k):
         assert np.array_equal(items[k], ref), f"shooter {p}: {np.count_nonzero(items[k] != ref)} px differ"
 
 
-@pytest.mark.parametrize("tile,small", [(64, 256), (32, 64)])
+@pytest.mark.parametrize("tile,small", [(64, 4096), (32, 64), (16, 1)])
 def test_room50k_ff_rows_bit_exact(lib, orc, room50k, tile, small):
     sh = _four_shooters(room50k)
     n = room50k["n"]
@@ -79,7 +79,7 @@ def test_room50k_ff_rows_bit_exact(lib, orc, room50k, tile, small):
 def test_room50k_shoot_k128_bit_exact(lib, orc, room50k):
     W, K, S = 512, 128, 2
     sc = room50k
-    with _solver(lib, sc, W, K, 1, tile=64, small_tri_pixels=256) as s:
+    with _solver(lib, sc, W, K, 1, tile=64, small_tri_pixels=4096) as s:
         st = s.shoot(S)
         rad, ill = s.download()
     assert st.shots_done == S and st.hemicubes == S * K
