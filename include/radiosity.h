@@ -248,6 +248,31 @@ int rad_multi_shoot(rad_multi* m, uint32_t n_replays, uint32_t* stop_replay, dou
                     double* device_ms);
 int rad_multi_destroy(rad_multi* m);
 
+/* ---- Many scenes solved by learned warm start + BF16 gather under one CUDA graph ----------
+ * No counterpart in the reference.  Each context (PHYS mode, scene uploaded; its unshot
+ * energy is the emission E) is a branch of one captured graph: dense capture of its form
+ * factors, E and its norms, the first-shot direct light rho o (F E), the network's 32 features
+ * per patch and its guess (or, with mlp NULL, the guess E), the guess's residual, then the
+ * refinements of rad_gather_solve (`sweeps` BF16 tcgen05 sweeps, update, FP32 residual with
+ * FP64 norms) in a conditional loop that the device ends once the scene's relative residual
+ * max_c ||r_c|| / ||E_c|| <= tol or after max_outer refinements.  feature_dirs: the 8 x 3
+ * feature directions b_k of the sin / cos features (needed with an mlp).  Contexts must stay
+ * alive and unused elsewhere while the object exists; their dense rows stay readable
+ * (rad_dense_rows) after a run. */
+typedef struct rad_multi_gather rad_multi_gather;
+int rad_multi_gather_create(rad_ctx* const* ctxs, uint32_t count, const rad_mlp* mlp, const double* feature_dirs,
+                            double tol, uint32_t max_outer, uint32_t sweeps, rad_multi_gather** out);
+/* One graph launch: every scene solved.  Per scene (arrays of count, any may be NULL): the
+ * device ms from the graph's start to its final check, residual evaluations, final and
+ * initial relative residual, status (1 converged, 2 stopped by max_outer, 3 non-finite);
+ * *device_ms = the whole launch.  RAD_E_NUMERIC if a residual was not finite, RAD_E_TIMEOUT if
+ * a pipeline wait gave up, RAD_E_OVERFLOW on raster capacity. */
+int rad_multi_gather_run(rad_multi_gather* m, double* device_ms, double* scene_ms, uint32_t* outer,
+                         double* residual, double* initial_residual, uint32_t* status);
+/* Scene `index`'s radiosity after a run: 3 x N floats (channel-major, as rad_gather_solve). */
+int rad_multi_gather_result(rad_multi_gather* m, uint32_t index, float* radiosity);
+int rad_multi_gather_destroy(rad_multi_gather* m);
+
 /* Raster counters of the last rad_profile_stages call (8 values): record-bin pairs (a record
  * holds both triangles of a patch quad), small records (row spans), their box pixels, big
  * records (one warp per triangle), their 8x4 stamps, stamps visited, stamps wholly inside,

@@ -40,6 +40,7 @@ EXPORTS = [
     "rad_scene_reference_neighbours", "rad_scene_obj", "rad_rr_size", "rad_rr_write", "rad_rr_read",
     "rad_upload_neighbours", "rad_display_colors", "rad_display_colors_device", "rad_highest_patch", "rad_progress",
     "rad_set_progress", "rad_selftest_bounded_wait", "rad_face_cameras", "rad_profile_raster_phases",
+    "rad_multi_gather_create", "rad_multi_gather_run", "rad_multi_gather_result", "rad_multi_gather_destroy",
 ]
 STAGES = ["select", "camera", "setup", "bins", "raster", "update", "emitters"]
 STAGE_KERNELS = [1, 1, 1, 2, 1, 1, 1]
@@ -153,6 +154,11 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rad_multi_create.argtypes = [P(vp), ctypes.c_uint32, P(vp)]
     L.rad_multi_shoot.argtypes = [vp, ctypes.c_uint32, vp, vp, P(ctypes.c_uint32), P(ctypes.c_double)]
     L.rad_multi_destroy.argtypes = [vp]
+    L.rad_multi_gather_create.argtypes = [P(vp), ctypes.c_uint32, vp, vp, ctypes.c_double, ctypes.c_uint32,
+                                          ctypes.c_uint32, P(vp)]
+    L.rad_multi_gather_run.argtypes = [vp, P(ctypes.c_double), vp, vp, vp, vp, vp]
+    L.rad_multi_gather_result.argtypes = [vp, ctypes.c_uint32, _f32p]
+    L.rad_multi_gather_destroy.argtypes = [vp]
     L.rad_autotune.argtypes = [vp, ctypes.c_uint32, P(RadTuning)]
     L.rad_raster_counters.argtypes = [vp, np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")]
     L.rad_reduce_items_noalloc.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp, vp]
@@ -661,6 +667,65 @@ class Multi:
     def close(self):
         if self.h:
             self.L.rad_multi_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class MultiGather:
+    """rad_multi_gather: scenes solved together by (learned warm start +) BF16 gather under one
+    captured CUDA graph: dense capture, features, network guess and the refinement loop (a
+    conditional node) all run on the device; each scene stops at its own tolerance."""
+
+    def __init__(self, solvers, mlp=None, tol: float = 1e-4, max_outer: int = 100, sweeps: int = 4):
+        self.L = load()
+        self.solvers = list(solvers)
+        arr = (ctypes.c_void_p * len(self.solvers))(*[s.h.value for s in self.solvers])
+        dirs = None
+        if mlp is not None:
+            from .learned import _FOURIER
+
+            self._dirs = np.ascontiguousarray(_FOURIER, np.float64)
+            dirs = self._dirs.ctypes.data_as(ctypes.c_void_p)
+        h = ctypes.c_void_p()
+        rc = self.L.rad_multi_gather_create(arr, len(self.solvers), mlp.h if mlp is not None else None, dirs, tol,
+                                            max_outer, sweeps, ctypes.byref(h))
+        if rc:
+            raise RadError(rc, "rad_multi_gather_create")
+        self.h = h
+
+    def run(self) -> dict:
+        n = len(self.solvers)
+        ms = ctypes.c_double()
+        scene_ms = np.zeros(n, np.float64)
+        outer = np.zeros(n, np.uint32)
+        res = np.zeros(n, np.float64)
+        res0 = np.zeros(n, np.float64)
+        status = np.zeros(n, np.uint32)
+        ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        rc = self.L.rad_multi_gather_run(self.h, ctypes.byref(ms), ptr(scene_ms), ptr(outer), ptr(res), ptr(res0),
+                                         ptr(status))
+        if rc:
+            raise RadError(rc, "rad_multi_gather_run")
+        return {"device_ms": ms.value, "scene_ms": scene_ms, "outer": outer, "residual": res,
+                "initial_residual": res0, "status": status}
+
+    def result(self, i: int) -> np.ndarray:
+        """Scene i's radiosity as a 3 x N array (one row per channel)."""
+        n = self.solvers[i].n
+        out = np.zeros(3 * n, np.float32)
+        rc = self.L.rad_multi_gather_result(self.h, i, out)
+        if rc:
+            raise RadError(rc, "rad_multi_gather_result")
+        return out.reshape(3, n)
+
+    def close(self):
+        if self.h:
+            self.L.rad_multi_gather_destroy(self.h)
             self.h = None
 
     def __enter__(self):

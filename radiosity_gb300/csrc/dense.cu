@@ -780,6 +780,20 @@ static int launch_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv
     return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 
+// Shared-memory limits of the streaming residual and the tcgen05 GEMM instances, set before
+// the first launch (and so before any stream capture that contains them).
+cudaError_t dense_init() {
+    cudaError_t e = cudaFuncSetAttribute(k_resid_stream<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_resid_stream<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<16>::kSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<32>::kSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<64>::kSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<128>::kSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<192>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<192>::kSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<256>::kSmem);
+    return e;
+}
+
 // Bt must have Rpad = the template width rows (zero padded) and ld columns.
 int launch_gemm_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv_bfloat16* Bt, uint32_t Rpad,
                    const TcEpilogue& ep, cudaStream_t s) {

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "radiosity.h"
+#include "rad_internal.cuh"
 
 namespace {
 
@@ -216,6 +217,20 @@ static void mlp_backward(rad_mlp* m, uint32_t P) {
             k_bwd_dx<<<blocks, 128, 0, m->stream>>>(m->dact[l + 1], P, in, out, m->p16 + m->off.w[l], m->dact[l]);
     }
 }
+
+namespace rad {
+void mlp_forward_device(const rad_mlp* m, const float* X, uint32_t P, float* act0, float* act1, float* Y,
+                        cudaStream_t s) {
+    const unsigned blocks = (P + kRows - 1) / kRows;
+    const float* in = X;
+    for (int l = 0; l < kLayers; l++) {
+        float* out = l == kLayers - 1 ? Y : ((l & 1) ? act1 : act0);
+        k_fwd<<<blocks, 128, 0, s>>>(in, P, kDims[l], kDims[l + 1], m->p16 + m->off.w[l], m->p + m->off.b[l], out,
+                                     l < kLayers - 1);
+        in = out;
+    }
+}
+}  // namespace rad
 
 extern "C" {
 

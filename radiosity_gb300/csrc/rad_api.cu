@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "radiosity.h"
+#include "rad_ctx.cuh"
 #include "rad_internal.cuh"
 
 namespace rad {
@@ -26,52 +27,6 @@ void launch_power0(const float4* rad, const float* area, uint32_t n, DevState* s
 }
 
 using namespace rad;
-
-namespace {
-
-struct BatchBuf {
-    Batch b{};
-    uint32_t cap_k = 0;
-    bool has_items = false;
-};
-
-}  // namespace
-
-struct rad_ctx {
-    rad_config cfg{};
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    std::string err;
-    Geo geo{};
-    uint32_t n = 0;
-    float* d_verts = nullptr;
-    float4* d_color = nullptr;
-    float4* d_rho = nullptr;
-    float4* d_rad = nullptr;
-    float4* d_illum = nullptr;
-    float* d_area = nullptr;
-    uint32_t* d_nb = nullptr;      // display neighbours, N x 8 (rad_upload_neighbours)
-    float* d_shade = nullptr;      // display colour scratch, 2 x N x 12 (rad_display_colors)
-    unsigned long long* d_best = nullptr;  // argmax key (rad_highest_patch)
-    float* d_fftab = nullptr;
-    BinInfo* d_bins = nullptr;
-    DevState* d_state = nullptr;   // shoot loop state
-    DevState* d_aux = nullptr;     // state for the one-off entry points
-    uint32_t* h_flag = nullptr;    // pinned stop flag
-    float* d_f3 = nullptr;         // device scratch for the host's float3 arrays, 2 x 3N floats
-    BatchBuf shoot;                // K = hemicubes_count
-    BatchBuf aux;                  // one-off calls, grown on demand
-    float* d_rows = nullptr;       // float rows for ff_rows / reduce
-    size_t rows_cap = 0;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t graph_exec = nullptr;
-    // dense form factors (rad_dense_capture)
-    float* d_F32 = nullptr;
-    __nv_bfloat16* d_F16 = nullptr;
-    float* d_scale = nullptr;
-    uint32_t dense_ld = 0;
-    bool dense_ready = false;
-};
 
 #define RAD_CUDA(ctx, call)                                                                         \
     do {                                                                                            \
@@ -86,6 +41,7 @@ static int fail(rad_ctx* ctx, int code, const char* msg) {
     if (ctx) ctx->err = msg;
     return code;
 }
+int ctx_fail(rad_ctx* ctx, int code, const char* msg) { return fail(ctx, code, msg); }
 
 template <typename T>
 static void dfree(T*& p) {
@@ -124,6 +80,8 @@ static uint32_t list_cap_per_hemi(const rad_ctx* c) {
     return c->cfg.binref_capacity ? c->cfg.binref_capacity : 4u * tri_cap_per_hemi(c);
 }
 
+static int alloc_batch(rad_ctx* c, BatchBuf& bb, uint32_t K, bool items);
+int ctx_alloc_batch(rad_ctx* c, BatchBuf& bb, uint32_t K, bool items) { return alloc_batch(c, bb, K, items); }
 static int alloc_batch(rad_ctx* c, BatchBuf& bb, uint32_t K, bool items) {
     if (bb.cap_k >= K && (!items || bb.has_items) && bb.b.Fq) {
         bb.b.K = K;
@@ -353,7 +311,7 @@ int rad_create(const rad_config* cfg, rad_ctx** out) {
         return code;
     };
     if (cudaSetDevice(cfg->device) != cudaSuccess) return bail(RAD_E_CUDA);
-    if (raster_init() != cudaSuccess) return bail(RAD_E_CUDA);
+    if (raster_init() != cudaSuccess || dense_init() != cudaSuccess) return bail(RAD_E_CUDA);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(RAD_E_CUDA);
     if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) return bail(RAD_E_CUDA);
     std::vector<BinInfo> bins;
@@ -857,8 +815,11 @@ int rad_autotune(rad_ctx* c, uint32_t flags, rad_tuning* out) {
 // stream: the chunk's shooter ids are a slice of one device array of 0..n-1, the row
 // conversion zeroes the exact sums it has read (so the next chunk starts from zero), and
 // the capacity flags are read once at the end.
-int rad_dense_capture(rad_ctx* c, uint32_t flags, double* device_ms) {
-    if (!c) return RAD_E_INVALID;
+}  // extern "C"
+
+uint32_t ctx_dense_chunk(const rad_ctx* c) { return std::min<uint32_t>(128, c->n); }
+
+int ctx_dense_alloc(rad_ctx* c, bool fp32) {
     if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
     const uint32_t n = c->n, ld = (n + 63u) & ~63u;
     dfree(c->d_F32);
@@ -868,10 +829,46 @@ int rad_dense_capture(rad_ctx* c, uint32_t flags, double* device_ms) {
     c->dense_ld = ld;
     RAD_CUDA(c, cudaMalloc(&c->d_F16, sizeof(__nv_bfloat16) * (size_t)n * ld));
     RAD_CUDA(c, cudaMalloc(&c->d_scale, sizeof(float) * n));
-    if (flags & RAD_DENSE_FP32) RAD_CUDA(c, cudaMalloc(&c->d_F32, sizeof(float) * (size_t)n * ld));
-    const uint32_t chunk = std::min<uint32_t>(128, n);
+    if (fp32) RAD_CUDA(c, cudaMalloc(&c->d_F32, sizeof(float) * (size_t)n * ld));
+    const uint32_t chunk = ctx_dense_chunk(c);
     int rc = alloc_batch(c, c->aux, chunk, false);
     if (rc) return rc;
+    std::vector<uint32_t> ones(chunk, 1u);
+    Batch& b = c->aux.b;
+    RAD_CUDA(c, cudaMemcpyAsync(b.valid, ones.data(), sizeof(uint32_t) * chunk, cudaMemcpyHostToDevice, c->stream));
+    RAD_CUDA(c, cudaMemsetAsync(b.Fq, 0, sizeof(unsigned long long) * (size_t)chunk * n, c->stream));
+    RAD_CUDA(c, cudaStreamSynchronize(c->stream));
+    return RAD_OK;
+}
+
+// One hemicube per patch, `chunk` at a time: camera, setup, bins, raster with the fused
+// exact reduction, then k_dense_rows turns the chunk's exact sums into FP32 / BF16 rows and
+// clears them for the next chunk.
+void ctx_enqueue_dense_capture(rad_ctx* c, const uint32_t* d_ids, cudaStream_t s) {
+    const uint32_t n = c->n, chunk = ctx_dense_chunk(c);
+    Batch b = c->aux.b;
+    cudaMemsetAsync(c->d_aux, 0, sizeof(DevState), s);
+    for (uint32_t first = 0; first < n; first += chunk) {
+        const uint32_t cnt = std::min(chunk, n - first);
+        b.K = cnt;
+        b.shooters = const_cast<uint32_t*>(d_ids) + first;
+        cudaMemsetAsync(b.tri_counts, 0, sizeof(uint32_t) * cnt, s);
+        cudaMemsetAsync(b.bin_count, 0, sizeof(uint32_t) * (size_t)cnt * c->geo.nb, s);
+        launch_camera(c->geo, b, c->d_verts, c->d_rad, c->d_aux, s);
+        launch_setup(c->geo, b, c->d_verts, c->d_aux, s);
+        launch_bins(c->geo, b, c->d_aux, s);
+        launch_raster(c->geo, b, c->d_fftab, c->d_aux, false, true, s);
+        launch_dense_rows(b.Fq, cnt, n, c->dense_ld, first, c->d_F32, c->d_F16, c->d_scale, s);
+    }
+}
+
+extern "C" {
+
+int rad_dense_capture(rad_ctx* c, uint32_t flags, double* device_ms) {
+    if (!c) return RAD_E_INVALID;
+    int rc = ctx_dense_alloc(c, (flags & RAD_DENSE_FP32) != 0);
+    if (rc) return rc;
+    const uint32_t n = c->n;
     cudaStream_t s = c->stream;
     uint32_t* d_ids = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -881,28 +878,14 @@ int rad_dense_capture(rad_ctx* c, uint32_t flags, double* device_ms) {
         if (e1) cudaEventDestroy(e1);
         return code;
     };
-    std::vector<uint32_t> ids(n), ones(chunk, 1u);
+    std::vector<uint32_t> ids(n);
     for (uint32_t i = 0; i < n; i++) ids[i] = i;
     if (cudaMalloc(&d_ids, sizeof(uint32_t) * n) != cudaSuccess) return done(fail(c, RAD_E_NOMEM, "cudaMalloc ids"));
-    Batch b = c->aux.b;
     bool ok = cudaMemcpyAsync(d_ids, ids.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, s) == cudaSuccess &&
-              cudaMemcpyAsync(b.valid, ones.data(), sizeof(uint32_t) * chunk, cudaMemcpyHostToDevice, s) == cudaSuccess &&
-              cudaMemsetAsync(c->d_aux, 0, sizeof(DevState), s) == cudaSuccess &&
-              cudaMemsetAsync(b.Fq, 0, sizeof(unsigned long long) * (size_t)chunk * n, s) == cudaSuccess &&
               cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess &&
               cudaEventRecord(e0, s) == cudaSuccess;
-    for (uint32_t first = 0; ok && first < n; first += chunk) {
-        const uint32_t cnt = std::min(chunk, n - first);
-        b.K = cnt;
-        b.shooters = d_ids + first;
-        ok = cudaMemsetAsync(b.tri_counts, 0, sizeof(uint32_t) * cnt, s) == cudaSuccess &&
-             cudaMemsetAsync(b.bin_count, 0, sizeof(uint32_t) * (size_t)cnt * c->geo.nb, s) == cudaSuccess;
-        if (!ok) break;
-        launch_camera(c->geo, b, c->d_verts, c->d_rad, c->d_aux, s);
-        launch_setup(c->geo, b, c->d_verts, c->d_aux, s);
-        launch_bins(c->geo, b, c->d_aux, s);
-        launch_raster(c->geo, b, c->d_fftab, c->d_aux, false, true, s);
-        launch_dense_rows(b.Fq, cnt, n, ld, first, c->d_F32, c->d_F16, c->d_scale, s);
+    if (ok) {
+        ctx_enqueue_dense_capture(c, d_ids, s);
         ok = cudaGetLastError() == cudaSuccess;
     }
     ok = ok && cudaEventRecord(e1, s) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess;

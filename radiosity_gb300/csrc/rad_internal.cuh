@@ -177,7 +177,17 @@ void launch_axpy(float* y, const float* x, size_t total, cudaStream_t s);
 int launch_gemm_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv_bfloat16* Bt, uint32_t Rpad,
                    const TcEpilogue& ep, cudaStream_t s);
 uint32_t gemm_tc_width(uint32_t R);
+cudaError_t dense_init();  // per device, before the first residual / tcgen05 launch
 uint32_t gemm_tc_ksplit(uint32_t n, uint32_t ld, uint32_t R);  // K splits that fill the GPU best
 void launch_fftab(uint32_t W, float* fftab, cudaStream_t s);
 
+}  // namespace rad
+
+// mlp.cu: the warm-start network's forward pass on device rows (no allocation, no
+// synchronisation): X (P x 32, row-major) -> Y (P x 3); act0 / act1 hold P x 128 floats each.
+struct rad_mlp;
+namespace rad {
+void mlp_forward_device(const rad_mlp* m, const float* X, uint32_t P, float* act0, float* act1, float* Y,
+                        cudaStream_t s);
+constexpr int kMlpIn = 32, kMlpHidden = 128, kMlpOut = 3;
 }  // namespace rad
