@@ -6,7 +6,7 @@ with ctypes.  Scene generators for the synthetic benchmark workloads live in
 ``radiosity_gb300.scenes``.
 """
 from ._lib import (  # noqa: F401
-    EXPORTS, MLP, MODE_PHYS, MODE_REF, Multi, RadConfig, RadError, RadGatherStats, RadStats, RadTuning, Solver, bf16_gemm,
+    EXPORTS, MLP, MODE_PHYS, MODE_REF, Multi, MultiGather, RadConfig, RadError, RadGatherStats, RadStats, RadTuning, Solver, bf16_gemm,
     default_config, derived, load, obj_scene, plan_shooters, reference_neighbours,
     reference_scene, rr_read, rr_write, selftest_bounded_wait,
 )
