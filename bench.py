@@ -73,7 +73,9 @@ def parse():
     p.add_argument("--train-epochs", type=int, default=50, help="learned: training epochs")
     p.add_argument("--eval-scenes", type=int, default=100, help="learned: held-out room scenes")
     p.add_argument("--eval-patches", type=int, default=50000, help="learned: patch target of a held-out room")
-    p.add_argument("--learned-w", type=int, default=128, help="learned: hemicube side of training and evaluation")
+    p.add_argument("--learned-w", type=int, default=128, help="learned: hemicube side of the training captures")
+    p.add_argument("--eval-w", type=int, default=512, help="learned: hemicube side of the held-out evaluation")
+    p.add_argument("--save-weights", default="", help="learned: write the trained network here (.npz)")
     p.add_argument("--gen-workers", type=int, default=8, help="learned: scene-generation processes")
     return p.parse_args()
 
@@ -506,17 +508,20 @@ def run_learned(args):
     from radiosity_gb300 import learned
 
     lo, hi = (int(v) for v in args.train_patches.split(","))
-    W = args.learned_w
+    W, We = args.learned_w, args.eval_w
     m, training = train_warm_start(args, scenes_n=args.train_scenes, epochs=args.train_epochs, patches=(lo, hi),
                                    kinds=("room", "cornell"), sample=args.train_sample, W=W,
                                    workers=args.gen_workers)
+    if args.save_weights:
+        learned.save_network(m, args.save_weights, {"training": training, "features": "learned.features",
+                                                   "network": "32-128x4-3 ReLU, BF16 weights"})
     names = ("emission", "direct", "learned")
     rows, caps, npat = [], [], []
     t0 = time.perf_counter()
     specs = [("room", args.eval_patches, 10_000 + k, 40, 4) for k in range(args.eval_scenes)]
     for sc in learned.generated(specs, args.gen_workers):
         c0 = time.perf_counter()
-        with learned.capture(sc, W=W) as s:
+        with learned.capture(sc, W=We) as s:
             caps.append(time.perf_counter() - c0)
             npat.append(sc["n"])
             E = learned.emission_block(sc)
@@ -547,13 +552,13 @@ def run_learned(args):
             "speedup_vs_emission": summ["emission"]["solve_ms_mean"] / summ["learned"]["solve_ms_mean"],
             "speedup_vs_direct": summ["direct"]["solve_ms_mean"] / summ["learned"]["solve_ms_mean"],
             "training": training,
-            "evaluation": {"scenes": len(rows), "patches_mean": float(np.mean(npat)), "W": W,
+            "evaluation": {"scenes": len(rows), "patches_mean": float(np.mean(npat)), "W": We,
                            "capture_s_mean": float(np.mean(caps)), "wall_s": eval_s},
             "config": {"workload": f"MLP 32-128x4-3 BF16; trained on {args.train_scenes} solver-generated scenes "
                                    f"(rooms and Cornell variants, {lo}-{hi} patches, W={W}, {args.train_sample} "
                                    f"patches sampled per scene); evaluated on {args.eval_scenes} held-out seeded "
                                    f"rooms (20x20x5 m, 40 boxes, 4 ceiling emitters, {args.eval_patches} patches, "
-                                   f"W={W})"},
+                                   f"W={We})"},
             "data": "synthetic"}
     print(json.dumps(line), flush=True)
 

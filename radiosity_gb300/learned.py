@@ -14,11 +14,34 @@ The prediction only seeds rad_gather_solve, which still iterates to its toleranc
 """
 from __future__ import annotations
 
+import json
+import os
+
 import numpy as np
 
 from . import _lib, scenes
 
 _FOURIER = np.random.default_rng(1234).normal(0.0, 2.0, (8, 3)).astype(np.float64)
+
+# The network trained on solver-generated scenes by ``bench.py --workload learned
+# --save-weights`` (its training set and evaluation are recorded in the file's metadata).
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "warm_start_mlp.npz")
+
+
+def save_network(mlp: "_lib.MLP", path: str, meta: dict) -> None:
+    """FP32 master parameters and a JSON description of how they were trained."""
+    os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+    np.savez(path, params=mlp.params(), meta=np.array(json.dumps(meta)))
+
+
+def load_network(path: str = WEIGHTS, device: int = 0):
+    """(MLP, metadata) of a saved network, or None when the file is absent."""
+    if not os.path.exists(path):
+        return None
+    z = np.load(path, allow_pickle=False)
+    m = _lib.MLP(seed=0, device=device)
+    m.set_params(z["params"])
+    return m, json.loads(str(z["meta"]))
 
 
 def patch_geometry(vertices: np.ndarray):
