@@ -488,15 +488,21 @@ def train_warm_start(args, scenes_n: int = 48, epochs: int = 200, patches=(2000,
 
 
 def learned_headline(args):
-    """Time to residual <= 1e-4 on a 50k-patch Cornell variant: learned + BF16 gather vs plain FP32
-    shooter (see headline()), with the network trained first by this library's kernels."""
-    m, training = train_warm_start(args)
+    """Time to residual <= 1e-4 on two 50k-patch scenes -- the large configuration's room
+    (reflectance U[0.1, 0.8]) and a Cornell variant (grey walls 0.73, the harder case for a
+    shooter) -- learned warm start + BF16 gather vs the plain FP32 shooter (see headline())."""
+    from radiosity_gb300 import scenes
+
+    m, training = warm_start_network(args)
     try:
-        h = headline(args, m)
+        out = {}
+        for name, sc in (("room", scenes.room_with_boxes(target=args.headline_patches, seed=args.seed)),
+                         ("cornell", scenes.cornell_variant(args.headline_patches, seed=424242))):
+            out[name] = headline(args, m, sc)
     finally:
         m.close()
-    h["training"] = training
-    return h
+    out["training"] = training
+    return out
 
 
 def run_learned(args):
@@ -563,7 +569,7 @@ def run_learned(args):
     print(json.dumps(line), flush=True)
 
 
-def headline(args, m):
+def headline(args, m, sc):
     """Time to residual <= 1e-4 on one large scene: learned warm start + BF16 gather (dense capture
     included) against the plain FP32 progressive shooter, both at W=args.w on this GPU.
 
@@ -574,9 +580,8 @@ def headline(args, m):
     16 batches with its total radiosity (shot + unshot) checked after each (untimed); its own
     unshot-power rule is recorded beside it.  Final answers are checked in FP64 on the host."""
     import radiosity_gb300 as R
-    from radiosity_gb300 import learned, scenes
+    from radiosity_gb300 import learned
 
-    sc = scenes.cornell_variant(args.headline_patches, seed=424242)
     n, W, tol = sc["n"], args.w, 1e-4
     E = learned.emission_block(sc)
     E64 = E.T.astype(np.float64)
@@ -652,31 +657,61 @@ def headline(args, m):
             "gather_from_emission": {"solve_s": st0.device_ms / 1000, "outer": st0.outer, "sweeps": st0.sweeps,
                                      "initial_residual": st0.initial_residual},
             "answers_rel_l2_difference": rel_diff,
+            "capture_us_per_row": cap_ms * 1000 / n, "shoot_us_per_hemicube": dev_ms * 1000 / max(1, hemis),
+            "shooter_hemicubes_per_patch": hemis / n,
             "speedup_learned_gather_vs_plain": (dev_ms / 1000) / learned_s}
 
 
-def run_uneven(args):
-    """Uneven batch: 256 Cornell-variant scenes, patches log-uniform in [500, 8000], 1-3 lights.
+def warm_start_network(args):
+    """The shipped network (radiosity_gb300/data) with its training record, else one trained here
+    on 48 Cornell variants (2k-6k patches) with the training time reported."""
+    from radiosity_gb300 import learned
 
-    Plain FP32 shooter: all scenes under one captured CUDA graph, each to unshot fraction <= tol.
-    Learned warm start + BF16 gather: the same scenes one after another (dense capture, MLP guess,
-    gather to residual <= tol), timed with the host work (uploads, features) included; FP64
-    residuals of a few scenes are checked on the host."""
+    got = learned.load_network()
+    if got is not None:
+        m, meta = got
+        return m, dict(meta.get("training", {}), source="shipped network " + os.path.relpath(learned.WEIGHTS, ROOT))
+    m, training = train_warm_start(args)
+    return m, dict(training, source="trained in this run")
+
+
+def _rel_residual(r, E):
+    """max over channels of ||r_c|| / ||E_c|| (channels with E_c = 0 skipped); r, E: 3 x N."""
+    nE = np.linalg.norm(E.astype(np.float64), axis=1)
+    nr = np.linalg.norm(r.astype(np.float64), axis=1)
+    return float(np.max(nr[nE > 0] / nE[nE > 0]))
+
+
+def run_uneven(args):
+    """Uneven batch: 256 Cornell-variant scenes, patches log-uniform in [500, 8000], 1-3 lights, W=128.
+
+    Both arms run under one captured CUDA graph, and both stop each scene by the same rule: the
+    relative residual max_c ||r_c|| / ||E_c|| of the scene's own discrete system <= tol, on its
+    captured FP32 form-factor rows.
+      * Plain FP32 shooter (rad_multi): one replay advances every scene by one batch.  The graph
+        is replayed in segments of 16 and each open scene's own-system residual (the reciprocity
+        form of the shoot update) is checked after each segment, untimed; a scene's time is the
+        device time to the end of the segment in which it met the rule.
+      * Learned warm start + BF16 gather (rad_multi_gather): one graph launch captures every
+        scene's form factors, computes its features and network guess, and runs its refinement
+        loop on the device until its residual <= tol; a scene's time runs from the launch to its
+        final check.
+    The network's training is reported separately (the shipped network's record, or this run's)."""
     import radiosity_gb300 as R
     from radiosity_gb300 import learned, scenes
 
     rng = np.random.default_rng(args.seed)
-    n_scenes, W, tol = 256, 128, args.uneven_tol
+    n_scenes, W, tol, seg = 256, 128, args.uneven_tol, 16
     scs = []
     for k in range(n_scenes):
         target = int(np.exp(rng.uniform(np.log(500), np.log(8000))))
         scs.append(scenes.cornell_variant(target, seed=int(rng.integers(1 << 30)), n_lights=int(rng.integers(1, 4))))
     sizes = [sc["n"] for sc in scs]
-    # shooters per batch sized per scene so that all scenes need about the same number of replays
+    Es = [learned.emission_block(sc) for sc in scs]
     ks = R.plan_shooters(sizes, hemicubes_per_patch=2.0 if tol >= 1e-2 else 4.5)
 
     def make(sc, K, **kw):
-        s = R.Solver(hemicube_side=W, hemicubes_count=K, mode=R.MODE_PHYS, tolerance=tol, **kw)
+        s = R.Solver(hemicube_side=W, hemicubes_count=K, mode=R.MODE_PHYS, **kw)
         s.upload(sc["vertices"], sc["color"], sc["radiosity"], sc["illumination"], reflectance=sc["reflectance"])
         return s
 
@@ -685,96 +720,82 @@ def run_uneven(args):
     probe = make(scs[big], ks[big])
     tune = probe.autotune()
     probe.close()
-    solvers = [make(sc, K, tile=tune.tile, small_tri_pixels=tune.small_tri_pixels) for sc, K in zip(scs, ks)]
+    shape = dict(tile=tune.tile, small_tri_pixels=tune.small_tri_pixels)
+    # ---- plain shooter under one graph (device stop rule off: the residual rule stops it)
+    solvers = [make(sc, K, tolerance=1e-12, **shape) for sc, K in zip(scs, ks)]
+    for s in solvers:  # the FP32 rows for the residual rule (untimed)
+        s.dense_capture(keep_fp32=True)
+    t_done = np.zeros(n_scenes)
+    reps_done = np.zeros(n_scenes, np.int64)
+    res_plain = np.ones(n_scenes)
+    dev_ms, reps, t_check = 0.0, 0, 0.0
+    open_ = set(range(n_scenes))
     with R.Multi(solvers) as mm:
-        at, ms, reps, total = mm.shoot(4000)
-    done = at > 0
-    line = {"metric": f"scenes/s (plain shooter to unshot fraction <= {tol:g}, one CUDA graph)",
-            "value": float(done.sum()) / (total / 1000), "unit": "scenes/s", "workload": "uneven",
-            "higher_is_better": True, "scenes": n_scenes, "converged": int(done.sum()), "replays": reps,
-            "device_s": total / 1000, "per_scene_ms": {"p50": float(np.percentile(ms[done], 50)),
-                                                       "p99": float(np.percentile(ms[done], 99))},
-            "patches": {"min": int(min(sizes)), "max": int(max(sizes)), "total": int(sum(sizes))},
-            "hemicubes": int(sum(int(a) * k for a, k in zip(at, ks))),
-            "config": {"workload": f"{n_scenes} Cornell-variant scenes, W={W}, K per scene {min(ks)}-{max(ks)} "
-                                   f"(plan_shooters), tol={tol:g}", "tile_from_autotune": tune.tile}, "data": "synthetic"}
+        while open_ and reps < 4000:
+            _, _, r, ms = mm.shoot(seg)
+            dev_ms += ms
+            reps += r
+            c0 = time.perf_counter()
+            for i in sorted(open_):
+                rad, ill = solvers[i].download()
+                B = np.ascontiguousarray((rad + ill).reshape(-1, 3).T)
+                res_plain[i] = _rel_residual(solvers[i].shoot_residual(Es[i], B), Es[i])
+                if res_plain[i] <= tol:
+                    t_done[i], reps_done[i] = dev_ms, reps
+                    open_.discard(i)
+            t_check += time.perf_counter() - c0
+    plain_done = np.array([i not in open_ for i in range(n_scenes)])
     for s in solvers:
         s.close()
-    if not args.no_headline:
-        try:
-            line["learned_gather"] = uneven_gather(args, scs, tol, tune)
-            line["speedup_learned_gather_vs_plain_scenes_per_s"] = \
-                line["learned_gather"]["scenes_per_s"] / line["value"]
-        except Exception as e:
-            line["learned_gather"] = {"error": f"{type(e).__name__}: {e}"}
-    print(json.dumps(line), flush=True)
-
-
-def uneven_gather(args, scs, tol, tune, checks: int = 4, workers: int = 4):
-    """The uneven batch by learned warm start + BF16 gather: `workers` host threads take the
-    scenes in turn, each with its own context (its own CUDA stream), so one scene's host work
-    (upload, features) overlaps other scenes' GPU work.  The shared network is used under a
-    lock.  FP64 residuals of the first `checks` scenes are computed on the host after the pool."""
-    import threading
-    from concurrent.futures import ThreadPoolExecutor
-
-    import radiosity_gb300 as R
-    from radiosity_gb300 import learned
-
-    m, training = train_warm_start(args)
-    mlp_lock = threading.Lock()
-
-    def solve(k):
-        sc = scs[k]
-        t0 = time.perf_counter()
-        s = R.Solver(hemicube_side=128, hemicubes_count=16, mode=R.MODE_PHYS, tile=tune.tile,
-                     small_tri_pixels=tune.small_tri_pixels)
-        try:
-            s.upload(sc["vertices"], sc["color"], sc["radiosity"], sc["illumination"], reflectance=sc["reflectance"])
-            cap_ms = s.dense_capture(keep_fp32=True)
-            E = learned.emission_block(sc)
-            direct = learned.direct_light(s, E)
-            with mlp_lock:
-                guess = learned.warm_start(m, sc, direct)
-            B, st = s.gather(E, guess=guess, tol=tol, max_outer=100, sweeps=4)
-            wall = time.perf_counter() - t0
-            # the FP32 rows of checked scenes are kept for the FP64 check after the pool (host
-            # BLAS is not called from several threads at once)
-            keep = (s.dense_rows(0, sc["n"])[0], E, B) if k < checks else None
-            return wall, cap_ms / 1000 + st.device_ms / 1000, st.outer, keep
-        finally:
-            s.close()
-
-    def fp64_check(k, keep):
-        """FP64 residual of the gather system on the FP32 rows."""
-        F, E, B = keep
-        n = scs[k]["n"]
-        rho = scs[k]["reflectance"].reshape(n, 3).astype(np.float64)
-        E64 = E.T.astype(np.float64)
-        Bd = B.T.astype(np.float64)
-        r = E64 + rho * (F.astype(np.float64) @ Bd) - Bd
-        return float(np.max(np.linalg.norm(r, axis=0) / np.maximum(np.linalg.norm(E64, axis=0), 1e-30)))
-
-    t_all = time.perf_counter()
+    plain = {"scenes_per_s": float(plain_done.sum()) / (dev_ms / 1000), "device_s": dev_ms / 1000,
+             "converged": int(plain_done.sum()), "replays": reps,
+             "per_scene_ms": {"p50": float(np.percentile(t_done[plain_done], 50)),
+                              "p99": float(np.percentile(t_done[plain_done], 99))},
+             "hemicubes": int(sum(int(r) * k for r, k in zip(reps_done, ks))),
+             "residual_max": float(res_plain[plain_done].max()), "check_wall_s_untimed": t_check,
+             "K_per_scene": [int(min(ks)), int(max(ks))]}
+    # ---- learned warm start + BF16 gather under one graph
+    m, training = warm_start_network(args)
+    ctxs = [make(sc, 16, **shape) for sc in scs]
     try:
-        with ThreadPoolExecutor(max_workers=workers) as ex:
-            res = list(ex.map(solve, range(len(scs))))
+        t0 = time.perf_counter()
+        mg = R.MultiGather(ctxs, mlp=m, tol=tol, max_outer=100, sweeps=4)
+        build_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        out = mg.run()
+        wall = time.perf_counter() - t0
+        fp64 = []
+        for i in range(4):  # FP64 residual of the gather system on the FP32 rows
+            n = sizes[i]
+            F, _, _ = ctxs[i].dense_rows(0, n)
+            B = mg.result(i).T.astype(np.float64)
+            E64 = Es[i].T.astype(np.float64)
+            rho = scs[i]["reflectance"].reshape(n, 3).astype(np.float64)
+            fp64.append(_rel_residual((E64 + rho * (F.astype(np.float64) @ B) - B).T, Es[i]))
+        mg.close()
     finally:
+        for c in ctxs:
+            c.close()
         m.close()
-    total = time.perf_counter() - t_all
-    wall = [r[0] for r in res]
-    dev = [r[1] for r in res]
-    outer = [r[2] for r in res]
-    fp64 = [fp64_check(k, r[3]) for k, r in enumerate(res) if r[3] is not None]
-    return {"scenes_per_s": len(scs) / total, "wall_s": total, "host_threads": workers,
-            "per_scene_s": {"p50": float(np.percentile(wall, 50)), "p99": float(np.percentile(wall, 99))},
-            "per_scene_device_s": {"p50": float(np.percentile(dev, 50)), "p99": float(np.percentile(dev, 99))},
-            "refinements_mean": float(np.mean(outer)), "hemicubes": int(sum(sc["n"] for sc in scs)),
-            "fp64_residual_max_checked": float(np.max(fp64)) if fp64 else None, "fp64_checked_scenes": len(fp64),
-            "tol": tol, "training": training,
-            "note": f"{workers} host threads, one context (stream) per scene in flight; per-scene times run from "
-                    "the scene's start (upload) to its solution, the FP64 check excluded; the plain shooter's "
-                    "per-scene times run concurrently under one graph"}
+    ok = out["status"] == 1
+    gather = {"scenes_per_s": float(ok.sum()) / (out["device_ms"] / 1000), "device_s": out["device_ms"] / 1000,
+              "wall_s": wall, "graph_build_s": build_s, "converged": int(ok.sum()),
+              "per_scene_ms": {"p50": float(np.percentile(out["scene_ms"], 50)),
+                               "p99": float(np.percentile(out["scene_ms"], 99))},
+              "refinements_mean": float(np.mean(out["outer"]) - 1), "residual_max": float(out["residual"].max()),
+              "initial_residual_mean": float(np.mean(out["initial_residual"])),
+              "fp64_residual_max_checked": max(fp64), "fp64_checked_scenes": len(fp64),
+              "hemicubes": int(sum(sizes)), "training": training}
+    line = {"metric": f"scenes/s to own-system relative residual <= {tol:g} (256 uneven scenes, one CUDA graph each arm)",
+            "value": gather["scenes_per_s"], "unit": "scenes/s", "workload": "uneven", "higher_is_better": True,
+            "scenes": n_scenes, "patches": {"min": int(min(sizes)), "max": int(max(sizes)), "total": int(sum(sizes))},
+            "learned_gather": gather, "plain_shooter": plain,
+            "speedup_learned_gather_vs_plain": gather["scenes_per_s"] / plain["scenes_per_s"],
+            "config": {"workload": f"{n_scenes} Cornell-variant scenes, 500-8000 patches (log-uniform), 1-3 lights, "
+                                   f"W={W}, tol={tol:g}", "tile_from_autotune": tune.tile,
+                       "small_tri_pixels_from_autotune": tune.small_tri_pixels},
+            "data": "synthetic"}
+    print(json.dumps(line), flush=True)
 
 
 def main():
