@@ -71,6 +71,8 @@ def parse():
     p.add_argument("--train-patches", default="5000,50000", help="learned: training patch range (log-uniform)")
     p.add_argument("--train-sample", type=int, default=2048, help="learned: patches kept per training scene")
     p.add_argument("--train-epochs", type=int, default=50, help="learned: training epochs")
+    p.add_argument("--train-batch", type=int, default=4096, help="warm-start network: rows per Adam step")
+    p.add_argument("--train-lr", type=float, default=2e-3, help="warm-start network: Adam learning rate")
     p.add_argument("--eval-scenes", type=int, default=100, help="learned: held-out room scenes")
     p.add_argument("--eval-patches", type=int, default=50000, help="learned: patch target of a held-out room")
     p.add_argument("--learned-w", type=int, default=128, help="learned: hemicube side of the training captures")
@@ -481,10 +483,14 @@ def train_warm_start(args, scenes_n: int = 48, epochs: int = 200, patches=(2000,
     order = np.random.default_rng(args.seed).permutation(X.shape[0])  # batches mix scenes
     X, T = np.ascontiguousarray(X[order]), np.ascontiguousarray(T[order])
     m = R.MLP(seed=args.seed)
-    loss, train_ms = m.train(X, T, epochs=epochs, batch=4096, lr=2e-3)
+    batch, lr = args.train_batch, args.train_lr
+    loss, train_ms = m.train(X, T, epochs=epochs, batch=batch, lr=lr)
+    # forward + backward: 3 passes of 2 * (32*128 + 3*128*128 + 128*3) flop per sample
+    flop = 6.0 * sum(a * b for a, b in zip(R.MLP.DIMS[:-1], R.MLP.DIMS[1:])) * X.shape[0] * epochs
     return m, {"scenes": scenes_n, "kinds": list(kinds), "patch_range": list(patches), "W": W,
-               "samples": int(X.shape[0]), "sample_per_scene": sample, "epochs": epochs, "final_loss": loss,
-               "train_ms": train_ms, "data_gen_s": gen_s}
+               "samples": int(X.shape[0]), "sample_per_scene": sample, "epochs": epochs, "batch": batch, "lr": lr,
+               "final_loss": loss, "train_ms": train_ms, "train_tflops": flop / (train_ms * 1e9),
+               "engine": "tcgen05 BF16 GEMMs", "data_gen_s": gen_s}
 
 
 def learned_headline(args):

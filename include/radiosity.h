@@ -229,6 +229,11 @@ int rad_mlp_set_params(rad_mlp* mlp, const float* params);
 int rad_mlp_predict(rad_mlp* mlp, const float* X, uint32_t P, float* Y);
 /* Mean-squared-error loss of (X, T) and its gradient w.r.t. every parameter (no update). */
 int rad_mlp_gradients(rad_mlp* mlp, const float* X, const float* T, uint32_t P, float* grads, double* loss);
+/* Selects the engine of predict / gradients / train: on (the default) = tcgen05 tensor cores
+ * (every layer a BF16 GEMM with FP32 accumulation in TMEM, activations and output gradients
+ * rounded to BF16 between layers, bias / ReLU / ReLU-mask fused into the GEMM epilogues, weight
+ * gradients by split-K GEMMs over the batch); off = CUDA cores with FP32 activations. */
+int rad_mlp_set_tensor_cores(rad_mlp* mlp, int on);
 /* Adam epochs over (X, T) in consecutive batches; the data set is copied to the device once. */
 int rad_mlp_train(rad_mlp* mlp, const float* X, const float* T, uint32_t P, uint32_t epochs, uint32_t batch,
                   float lr, double* final_loss, double* device_ms);

@@ -27,25 +27,34 @@ def unpack(params: np.ndarray):
     return Ws, bs
 
 
-def forward(params, X):
+def _round(a, on):
+    return bf16_round(np.asarray(a, np.float32)).astype(np.float64) if on else a
+
+
+def forward(params, X, bf16_acts: bool = False):
+    """Layer inputs and the output.  bf16_acts: the input and every hidden activation rounded to
+    BF16, as the tensor-core engine feeds them to its GEMMs."""
     Ws, bs = unpack(params)
-    acts = [np.asarray(X, np.float64)]
+    acts = [_round(np.asarray(X, np.float64), bf16_acts)]
     for l in range(5):
         z = acts[-1] @ bf16_round(Ws[l]).astype(np.float64).T + bs[l].astype(np.float64)
-        acts.append(np.maximum(z, 0) if l < 4 else z)
+        acts.append(_round(np.maximum(z, 0), bf16_acts) if l < 4 else z)
     return acts
 
 
-def gradients(params, X, T):
+def gradients(params, X, T, bf16_acts: bool = False):
+    """MSE gradients; bf16_acts also rounds every layer's output gradient dZ to BF16 (the
+    tensor-core engine's GEMM operand) before it is used."""
     Ws, bs = unpack(params)
-    acts = forward(params, X)
+    acts = forward(params, X, bf16_acts)
     P = X.shape[0]
     d = 2.0 * (acts[-1] - np.asarray(T, np.float64)) / (P * 3)
     loss = float(np.mean((acts[-1] - T) ** 2))
     gW, gb = [None] * 5, [None] * 5
+    d = _round(d, bf16_acts)
     for l in range(4, -1, -1):
         if l < 4:
-            d = d * (acts[l + 1] > 0)
+            d = _round(d * (acts[l + 1] > 0), bf16_acts)
         gW[l] = d.T @ acts[l]
         gb[l] = d.sum(0)
         d = d @ bf16_round(Ws[l]).astype(np.float64)

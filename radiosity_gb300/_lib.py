@@ -41,6 +41,7 @@ EXPORTS = [
     "rad_upload_neighbours", "rad_display_colors", "rad_display_colors_device", "rad_highest_patch", "rad_progress",
     "rad_set_progress", "rad_selftest_bounded_wait", "rad_face_cameras", "rad_profile_raster_phases",
     "rad_multi_gather_create", "rad_multi_gather_run", "rad_multi_gather_result", "rad_multi_gather_destroy",
+    "rad_mlp_set_tensor_cores",
 ]
 STAGES = ["select", "camera", "setup", "bins", "raster", "update", "emitters"]
 STAGE_KERNELS = [1, 1, 1, 2, 1, 1, 1]
@@ -145,6 +146,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rad_mlp_create.argtypes = [ctypes.c_int, ctypes.c_uint64, P(vp)]
     L.rad_mlp_destroy.argtypes = [vp]
     L.rad_mlp_param_count.argtypes = []
+    L.rad_mlp_set_tensor_cores.argtypes = [vp, ctypes.c_int]
     L.rad_mlp_get_params.argtypes = [vp, _f32p]
     L.rad_mlp_set_params.argtypes = [vp, _f32p]
     L.rad_mlp_predict.argtypes = [vp, _f32p, ctypes.c_uint32, _f32p]
@@ -578,6 +580,12 @@ class MLP:
             self.close()
         except Exception:
             pass
+
+    def set_tensor_cores(self, on: bool) -> None:
+        """tcgen05 BF16 engine (default) or the CUDA-core FP32-activation engine."""
+        rc = self.L.rad_mlp_set_tensor_cores(self.h, 1 if on else 0)
+        if rc:
+            raise RadError(rc, "rad_mlp_set_tensor_cores")
 
     def params(self) -> np.ndarray:
         out = np.zeros(self.nparams, np.float32)

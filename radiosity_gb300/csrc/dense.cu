@@ -22,6 +22,9 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+
+#include <mutex>
+#include <unordered_map>
 #include <stdint.h>
 
 #include <cmath>
@@ -563,6 +566,64 @@ struct TcShape {
                                        ((uint32_t)(kTcM >> 4) << 24);
 };
 
+// One output element of the network modes (2-5) of TcEpilogue; y = the FP32 accumulator.
+__device__ __forceinline__ void net_store(const TcEpilogue& ep, uint32_t row, uint32_t c, float y) {
+    if (ep.mode == 3) {
+        ep.out[(size_t)row * ep.R + c] = y + ep.bias[c];
+        return;
+    }
+    if (ep.mode == 5) {
+        ep.out[(size_t)row * ep.ldr + c] = y;
+        return;
+    }
+    if (ep.mode == 2) y = fmaxf(y + ep.bias[c], 0.f);
+    else if (!(__bfloat162float(ep.mask[(size_t)row * ep.ldm + c]) > 0.f)) y = 0.f;  // mode 4
+    const __nv_bfloat16 h = __float2bfloat16_rn(y);
+    ep.out16r[(size_t)row * ep.ldr + c] = h;
+    ep.out16[(size_t)c * ep.ld16 + row] = h;
+}
+
+__device__ __forceinline__ void net_epilogue(const TcEpilogue& ep, uint32_t row, int c0, const uint32_t* v) {
+    if ((ep.mode == 2 || ep.mode == 4) && (uint32_t)c0 + 32u <= ep.R) {
+        // the row's 32 BF16 values go out as four 16-byte stores (and the mask comes in as four
+        // 16-byte loads); the column-major copy is one element per lane, 32 rows per store
+        uint4 mk[4];
+        if (ep.mode == 4) {
+            const uint4* ms = reinterpret_cast<const uint4*>(ep.mask + (size_t)row * ep.ldm + c0);
+#pragma unroll
+            for (int q = 0; q < 4; q++) mk[q] = ms[q];
+        }
+        const __nv_bfloat16* mh = reinterpret_cast<const __nv_bfloat16*>(mk);
+        uint32_t packed[16];
+#pragma unroll
+        for (int j = 0; j < 32; j += 2) {
+            float y0 = __uint_as_float(v[j]), y1 = __uint_as_float(v[j + 1]);
+            if (ep.mode == 2) {
+                y0 = fmaxf(y0 + ep.bias[c0 + j], 0.f);
+                y1 = fmaxf(y1 + ep.bias[c0 + j + 1], 0.f);
+            } else {
+                if (!(__bfloat162float(mh[j]) > 0.f)) y0 = 0.f;
+                if (!(__bfloat162float(mh[j + 1]) > 0.f)) y1 = 0.f;
+            }
+            const __nv_bfloat162 h = __floats2bfloat162_rn(y0, y1);
+            packed[j / 2] = *reinterpret_cast<const uint32_t*>(&h);
+            ep.out16[(size_t)(c0 + j) * ep.ld16 + row] = h.x;
+            ep.out16[(size_t)(c0 + j + 1) * ep.ld16 + row] = h.y;
+        }
+        uint4* dst = reinterpret_cast<uint4*>(ep.out16r + (size_t)row * ep.ldr + c0);
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            dst[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
+        return;
+    }
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+        const uint32_t c = (uint32_t)(c0 + j);
+        if (c >= ep.R) break;
+        net_store(ep, row, c, __uint_as_float(v[j]));
+    }
+}
+
 template <int NR>
 __global__ void __launch_bounds__(256, 1) k_gemm_tc(const __grid_constant__ CUtensorMap tmA,
                                                     const __grid_constant__ CUtensorMap tmB, uint32_t kblocks,
@@ -657,6 +718,10 @@ __global__ void __launch_bounds__(256, 1) k_gemm_tc(const __grid_constant__ CUte
                     : "r"(ta));
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 if (!live) continue;
+                if (nsplit == 1 && ep.mode >= 2) {
+                    net_epilogue(ep, row, c0, v);
+                    continue;
+                }
                 if (nsplit > 1) {  // raw partial sums; k_tc_finalize adds the splits in order
 #pragma unroll
                     for (int j = 0; j < 32; j++) {
@@ -728,8 +793,22 @@ __global__ void k_tc_finalize(TcEpilogue ep) {
     const size_t total = (size_t)ep.R * ep.n;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
         const uint32_t c = (uint32_t)(e / ep.n), row = (uint32_t)(e % ep.n);
+        // the splits' partial sums are loaded eight at a time (independent loads in flight)
+        // and added in split order
         float acc = 0.f;
-        for (uint32_t sp = 0; sp < ep.ksplit; sp++) acc += ep.partial[((size_t)sp * ep.R + c) * ep.n + row];
+        const size_t stride = (size_t)ep.R * ep.n, at = (size_t)c * ep.n + row;
+        for (uint32_t sp0 = 0; sp0 < ep.ksplit; sp0 += 8) {
+            float v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) v[u] = sp0 + u < ep.ksplit ? ep.partial[(sp0 + u) * stride + at] : 0.f;
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+                if (sp0 + u < ep.ksplit) acc += v[u];
+        }
+        if (ep.mode >= 2) {
+            net_store(ep, row, c, acc);
+            continue;
+        }
         const float sc = ep.scale ? ep.scale[row] : 1.0f;
         float y = sc * acc;
         if (ep.mode == 1) {
@@ -764,12 +843,50 @@ uint32_t gemm_tc_ksplit(uint32_t n, uint32_t ld, uint32_t R) {
     return best;
 }
 
+// Tensor maps by (base, rows, row length, box rows): a map depends on nothing else, so one
+// encoded for a buffer is reused by every later launch on the same buffer and shape (the
+// network's layers launch many small GEMMs, where encoding on the host per launch dominated).
+struct MapKey {
+    const void* base;
+    uint64_t rows, ld;
+    uint32_t box;
+    bool operator==(const MapKey& o) const { return base == o.base && rows == o.rows && ld == o.ld && box == o.box; }
+};
+struct MapKeyHash {
+    size_t operator()(const MapKey& k) const {
+        uint64_t h = reinterpret_cast<uintptr_t>(k.base) * 0x9E3779B97F4A7C15ull;
+        h ^= k.rows + 0x632BE59BD9B4E019ull + (h << 6) + (h >> 2);
+        h ^= k.ld + 0x85EBCA77C2B2AE63ull + (h << 6) + (h >> 2);
+        h ^= k.box + (h << 6) + (h >> 2);
+        return (size_t)h;
+    }
+};
+
+static bool cached_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t ld, uint32_t box_rows) {
+    static std::mutex mu;
+    static std::unordered_map<MapKey, CUtensorMap, MapKeyHash> cache;
+    const MapKey key{base, rows, ld, box_rows};
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) {
+            *m = it->second;
+            return true;
+        }
+    }
+    if (!make_map(m, base, rows, ld, box_rows)) return false;
+    std::lock_guard<std::mutex> lock(mu);
+    if (cache.size() > 65536) cache.clear();
+    cache.emplace(key, *m);
+    return true;
+}
+
 template <int NR>
 static int launch_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv_bfloat16* Bt, const TcEpilogue& ep,
                      cudaStream_t s) {
     using S = TcShape<NR>;
     CUtensorMap ma, mb;
-    if (!make_map(&ma, A, n, ld, kTcM) || !make_map(&mb, Bt, NR, ld, NR)) return -1;
+    if (!cached_map(&ma, A, n, ld, kTcM) || !cached_map(&mb, Bt, NR, ld, NR)) return -1;
     static const cudaError_t attr =
         cudaFuncSetAttribute(k_gemm_tc<NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::kSmem);
     if (attr != cudaSuccess) return -2;

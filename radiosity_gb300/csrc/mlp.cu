@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -22,6 +23,9 @@
 #include "rad_internal.cuh"
 
 namespace {
+
+using rad::launch_gemm_tc;
+using rad::TcEpilogue;
 
 constexpr int kIn = 32, kHid = 128, kOut = 3, kLayers = 5;
 constexpr int kRows = 32;  // patches per CTA tile
@@ -138,6 +142,30 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
     }
 }
 
+// Adam with the step count read on the device (ctr[0], already advanced for this step), for
+// the captured training step of the tensor-core engine.
+__global__ void k_adam_dev(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                           float* __restrict__ v, uint32_t n, float lr, float b1, float b2, float eps,
+                           const uint32_t* __restrict__ ctr, __nv_bfloat16* __restrict__ p16) {
+    const float step = (float)ctr[0];
+    const float bc1 = 1.f - powf(b1, step), bc2 = 1.f - powf(b2, step);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float np = p[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+        p[i] = np;
+        p16[i] = __float2bfloat16_rn(np);
+    }
+}
+
+// Step counters of a captured training step: ctr[0] = Adam steps, ctr[1] = batch within the
+// epoch's full batches (wraps after `full`).
+__global__ void k_step_begin(uint32_t* ctr) { ctr[0] += 1; }
+__global__ void k_step_end(uint32_t* ctr, uint32_t full) { ctr[1] = ctr[1] + 1 >= full ? 0 : ctr[1] + 1; }
+
 __global__ void k_to_bf16(const float* __restrict__ p, uint32_t n, __nv_bfloat16* __restrict__ p16) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         p16[i] = __float2bfloat16_rn(p[i]);
@@ -176,7 +204,278 @@ struct rad_mlp {
     float* dact[kLayers + 1] = {};
     float* tgt = nullptr;
     double* loss = nullptr;
+    // tensor-core engine (tcgen05 BF16 GEMMs, FP32 accumulation; see tc_forward / tc_backward)
+    bool tc = true;
+    uint32_t tc_cap = 0;                       // rows the tc buffers hold (a multiple of 64)
+    __nv_bfloat16* w16[kLayers] = {};          // W_l, [NRout][Kin] (zero padded)
+    __nv_bfloat16* wt16[kLayers] = {};         // W_l^T, [NRin][Kout] (zero padded)
+    __nv_bfloat16* ar[kLayers] = {};           // layer inputs, row-major [P][Kin]
+    __nv_bfloat16* ac[kLayers] = {};           // layer inputs, column-major [in][cap]
+    __nv_bfloat16* zr[kLayers] = {};           // output gradients dZ_l, row-major [P][Kout]
+    __nv_bfloat16* zc[kLayers] = {};           // dZ_l, column-major [out][cap]
+    float* y = nullptr;                        // network output, [P][3]
+    float* part = nullptr;                     // split-K partial sums of the weight gradients
+    uint32_t* ctr = nullptr;                   // device step counters of the captured training step
 };
+
+// ---- tensor-core engine --------------------------------------------------------------------
+// Each layer is a tcgen05 GEMM C = A Bt^T of k_gemm_tc (128-row tiles, TMA-fed, FP32 in
+// TMEM) with the layer's work fused into the epilogue:
+//   forward  Z_l = A_l W_l^T: A_l row-major BF16 [P][Kin], Bt = W_l [out][Kin]; epilogue
+//            bias + ReLU, BF16 written row-major (next A) and column-major (dW operand);
+//            the last layer writes FP32 Y = Z + b;
+//   dW_l     = dZ_l^T A_l: A = dZ_l column-major [out][P], Bt = A_l column-major [in][P],
+//            K = P split over CTAs (k_tc_finalize adds the splits in order);
+//   dX_l     = dZ_l W_l: A = dZ_l row-major [P][Kout], Bt = W_l^T [in][Kout]; epilogue
+//            masks with A_l > 0 (the ReLU of the layer below) and writes dZ_{l-1} in BF16,
+//            row- and column-major.
+// Activations and output gradients are BF16 (tensor-core operands), sums FP32; the FP32
+// master weights, biases, their gradients and Adam stay as in the CUDA-core engine.
+const uint32_t kKin[kLayers] = {64, 128, 128, 128, 128};      // in, padded to the 64-wide K block
+const uint32_t kKout[kLayers] = {128, 128, 128, 128, 64};     // out, padded likewise
+const uint32_t kNRout[kLayers] = {128, 128, 128, 128, 16};    // GEMM widths of out
+const uint32_t kNRin[kLayers] = {32, 128, 128, 128, 128};     // GEMM widths of in
+
+__device__ __forceinline__ uint32_t pad64(uint32_t x) { return (x + 63u) & ~63u; }
+
+// W_l -> w16 [NRout][Kin] and wt16 [NRin][Kout] (BF16, zero padded); layer = blockIdx.y.
+struct TcWeights {
+    __nv_bfloat16* w16[kLayers];
+    __nv_bfloat16* wt16[kLayers];
+    uint32_t wo[kLayers];
+};
+__global__ void k_tc_weights(const float* __restrict__ p, TcWeights tw) {
+    const int l = blockIdx.y;
+    const int in = l == 0 ? kIn : kHid, out = l == kLayers - 1 ? kOut : kHid;
+    const uint32_t kin = l == 0 ? 64u : 128u, kout = l == kLayers - 1 ? 64u : 128u;
+    const uint32_t nrout = l == kLayers - 1 ? 16u : 128u, nrin = l == 0 ? 32u : 128u;
+    const float* W = p + tw.wo[l];
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < 128u * 128u; e += gridDim.x * blockDim.x) {
+        if (e < nrout * kin) {
+            const uint32_t o = e / kin, k = e % kin;
+            tw.w16[l][e] = __float2bfloat16_rn((int)o < out && (int)k < in ? W[o * in + k] : 0.f);
+        }
+        if (e < nrin * kout) {
+            const uint32_t i = e / kout, o = e % kout;
+            tw.wt16[l][e] = __float2bfloat16_rn((int)o < out && (int)i < in ? W[o * in + i] : 0.f);
+        }
+    }
+}
+
+// The batch ctr[1] of a data set on the device: rows [ctr[1] * P, +P) of X -> A_0 (as
+// k_tc_input) and of T -> tgt.
+__global__ void k_tc_batch(const float* __restrict__ X, const float* __restrict__ T, uint32_t P, uint32_t K,
+                           const uint32_t* __restrict__ ctr, __nv_bfloat16* __restrict__ ar,
+                           __nv_bfloat16* __restrict__ ac, float* __restrict__ tgt) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= P * 64u) return;
+    const uint32_t r = e / 64u, k = e % 64u;
+    const size_t src = (size_t)ctr[1] * P + r;
+    const __nv_bfloat16 h = __float2bfloat16_rn(k < (uint32_t)kIn ? X[src * kIn + k] : 0.f);
+    ar[e] = h;
+    if (k < (uint32_t)kIn) ac[(size_t)k * K + r] = h;
+    if (k < (uint32_t)kOut) tgt[(size_t)r * kOut + k] = T[src * kOut + k];
+}
+
+// X (P x 32 FP32) -> A_0 row-major [P][64] and column-major [32][K] in BF16 (K = pad64(P),
+// the row pitch of every column-major buffer for this batch).
+__global__ void k_tc_input(const float* __restrict__ X, uint32_t P, uint32_t K, __nv_bfloat16* __restrict__ ar,
+                           __nv_bfloat16* __restrict__ ac) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= P * 64u) return;
+    const uint32_t r = e / 64u, k = e % 64u;
+    const __nv_bfloat16 h = __float2bfloat16_rn(k < (uint32_t)kIn ? X[(size_t)r * kIn + k] : 0.f);
+    ar[e] = h;
+    if (k < (uint32_t)kIn) ac[(size_t)k * K + r] = h;
+}
+
+// MSE: dY = 2 (Y - T) / (3P) in BF16 (row-major [P][64], column-major [3][K]); loss sum.
+__global__ void k_tc_mse(const float* __restrict__ Y, const float* __restrict__ T, uint32_t P, uint32_t K,
+                         __nv_bfloat16* __restrict__ zr, __nv_bfloat16* __restrict__ zc, double* loss) {
+    double part = 0;
+    const float scale = 2.0f / (float)((size_t)P * kOut);
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < P * (uint32_t)kOut; e += gridDim.x * blockDim.x) {
+        const uint32_t r = e / kOut, c = e % kOut;
+        const float d = Y[e] - T[e];
+        const __nv_bfloat16 h = __float2bfloat16_rn(scale * d);
+        zr[(size_t)r * 64 + c] = h;
+        zc[(size_t)c * K + r] = h;
+        part += (double)d * (double)d;
+    }
+    __shared__ double red[256];
+    red[threadIdx.x] = part;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(loss, red[0]);
+}
+
+// db_l[o] = sum over rows of dZ_l[r][o] (column-major BF16, pitch K), one CTA per output:
+// 8 rows per 16-byte load, four loads in flight per thread (K is a multiple of 64 and the
+// columns [P, K) are zero).
+__global__ void __launch_bounds__(256) k_tc_bias_grad(const __nv_bfloat16* __restrict__ zc, uint32_t K,
+                                                      float* __restrict__ db) {
+    const uint32_t o = blockIdx.x;
+    const uint4* src = reinterpret_cast<const uint4*>(zc + (size_t)o * K);
+    const uint32_t nv = K / 8u;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    for (uint32_t v0 = threadIdx.x; v0 < nv; v0 += 4u * blockDim.x) {
+        uint4 q[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const uint32_t v = v0 + (uint32_t)u * blockDim.x;
+            q[u] = v < nv ? src[v] : make_uint4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q[u]);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float2 f = __bfloat1622float2(h[j]);
+                acc[u] += f.x + f.y;
+            }
+        }
+    }
+    __shared__ float red[256];
+    red[threadIdx.x] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) db[o] = red[0];
+}
+
+static void tc_free_acts(rad_mlp* m) {
+    for (int l = 0; l < kLayers; l++) {
+        cudaFree(m->ar[l]); cudaFree(m->ac[l]); cudaFree(m->zr[l]); cudaFree(m->zc[l]);
+        m->ar[l] = m->ac[l] = m->zr[l] = m->zc[l] = nullptr;
+    }
+    cudaFree(m->y);
+    cudaFree(m->part);
+    m->y = nullptr;
+    m->part = nullptr;
+    m->tc_cap = 0;
+}
+
+constexpr uint32_t kDwSplits = 148;  // K splits of a weight-gradient GEMM (at most; about one per SM)
+constexpr uint32_t kMinRows = 128;  // GEMM operands hold at least one full 128-row tile
+
+// Activation buffers for batches of up to P rows (at least kMinRows, a multiple of 64).
+static int tc_ensure(rad_mlp* m, uint32_t P) {
+    const uint32_t cap = std::max(kMinRows, (P + 63u) & ~63u);
+    if (m->tc_cap >= cap) return RAD_OK;
+    tc_free_acts(m);
+    bool ok = true;
+    for (int l = 0; l < kLayers && ok; l++) {
+        ok = cudaMalloc(&m->ar[l], 2 * (size_t)cap * kKin[l]) == cudaSuccess &&
+             cudaMalloc(&m->ac[l], 2 * (size_t)kNRin[l] * cap) == cudaSuccess &&
+             cudaMalloc(&m->zr[l], 2 * (size_t)cap * kKout[l]) == cudaSuccess &&
+             cudaMalloc(&m->zc[l], 2 * (size_t)kMinRows * cap) == cudaSuccess;
+        // padding never written by the kernels stays zero (columns past `in` / `out` of the
+        // row-major buffers, rows past `out` of the column-major output gradients)
+        ok = ok && cudaMemset(m->ar[l], 0, 2 * (size_t)cap * kKin[l]) == cudaSuccess &&
+             cudaMemset(m->ac[l], 0, 2 * (size_t)kNRin[l] * cap) == cudaSuccess &&
+             cudaMemset(m->zr[l], 0, 2 * (size_t)cap * kKout[l]) == cudaSuccess &&
+             cudaMemset(m->zc[l], 0, 2 * (size_t)kMinRows * cap) == cudaSuccess;
+    }
+    ok = ok && cudaMalloc(&m->y, 4 * (size_t)cap * kOut) == cudaSuccess &&
+         cudaMalloc(&m->part, 4 * (size_t)kDwSplits * kHid * kHid) == cudaSuccess;
+    if (!ok) {
+        tc_free_acts(m);
+        return RAD_E_NOMEM;
+    }
+    m->tc_cap = cap;
+    return RAD_OK;
+}
+
+// BF16 copies of the weights for the tensor-core engine (after any change of the master).
+static void tc_refresh(rad_mlp* m) {
+    TcWeights tw{};
+    for (int l = 0; l < kLayers; l++) {
+        tw.w16[l] = m->w16[l];
+        tw.wt16[l] = m->wt16[l];
+        tw.wo[l] = (uint32_t)m->off.w[l];
+    }
+    k_tc_weights<<<dim3(16, kLayers), 256, 0, m->stream>>>(m->p, tw);
+}
+
+// Forward pass of the P rows staged by tc_stage (m->ar[0], m->ac[0]); output in m->y.
+static int tc_forward(rad_mlp* m, uint32_t P) {
+    const uint32_t K = (P + 63u) & ~63u;  // pitch of the column-major activations
+    for (int l = 0; l < kLayers; l++) {
+        TcEpilogue ep{};
+        ep.n = P;
+        ep.R = (uint32_t)kDims[l + 1];
+        ep.bias = m->p + m->off.b[l];
+        if (l < kLayers - 1) {
+            ep.mode = 2;
+            ep.out16r = m->ar[l + 1];
+            ep.ldr = kKin[l + 1];
+            ep.out16 = m->ac[l + 1];
+            ep.ld16 = K;
+        } else {
+            ep.mode = 3;
+            ep.out = m->y;
+        }
+        if (launch_gemm_tc(m->ar[l], std::max(P, kMinRows), kKin[l], m->w16[l], kNRout[l], ep, m->stream) != 0)
+            return RAD_E_CUDA;
+    }
+    return RAD_OK;
+}
+
+// Loss and every parameter gradient (into m->g) of the batch whose forward pass ran.
+static int tc_backward(rad_mlp* m, uint32_t P) {
+    const uint32_t K = (P + 63u) & ~63u;  // rows of the weight-gradient GEMMs (their K)
+    cudaMemsetAsync(m->loss, 0, sizeof(double), m->stream);
+    if (K > P)  // the weight-gradient GEMMs run K over pad64(P) columns: the tail must be zero
+        cudaMemset2DAsync(m->zc[kLayers - 1] + P, 2 * (size_t)K, 0, 2 * (size_t)(K - P), kOut, m->stream);
+    k_tc_mse<<<152, 256, 0, m->stream>>>(m->y, m->tgt, P, K, m->zr[kLayers - 1], m->zc[kLayers - 1], m->loss);
+    const uint32_t splits = std::min<uint32_t>(kDwSplits, K / 64u);
+    for (int l = kLayers - 1; l >= 0; l--) {
+        const uint32_t in = (uint32_t)kDims[l], out = (uint32_t)kDims[l + 1];
+        TcEpilogue ep{};  // dW_l = dZ_l^T A_l, K = rows (split)
+        ep.mode = 5;
+        ep.n = out;
+        ep.R = in;
+        ep.out = m->g + m->off.w[l];
+        ep.ldr = in;
+        ep.partial = splits > 1 ? m->part : nullptr;
+        ep.ksplit = splits;
+        if (launch_gemm_tc(m->zc[l], kMinRows, K, m->ac[l], kNRin[l], ep, m->stream) != 0) return RAD_E_CUDA;
+        k_tc_bias_grad<<<out, 256, 0, m->stream>>>(m->zc[l], K, m->g + m->off.b[l]);
+        if (l > 0) {  // dZ_{l-1} = (dZ_l W_l) o [A_l > 0]
+            TcEpilogue ex{};
+            ex.mode = 4;
+            ex.n = P;
+            ex.R = in;
+            ex.mask = m->ar[l];
+            ex.ldm = kKin[l];
+            ex.out16r = m->zr[l - 1];
+            ex.ldr = kKout[l - 1];
+            ex.out16 = m->zc[l - 1];
+            ex.ld16 = K;
+            if (K > P)
+                cudaMemset2DAsync(m->zc[l - 1] + P, 2 * (size_t)K, 0, 2 * (size_t)(K - P), in, m->stream);
+            if (launch_gemm_tc(m->zr[l], std::max(P, kMinRows), kKout[l], m->wt16[l], kNRin[l], ex, m->stream) != 0)
+                return RAD_E_CUDA;
+        }
+    }
+    return RAD_OK;
+}
+
+// Stages P rows of X (device) for the tensor-core passes and zeroes the columns [P, K) of the
+// column-major activations (the weight-gradient GEMMs read them; an earlier, larger batch
+// may have left values there).
+static void tc_stage(rad_mlp* m, const float* dX, uint32_t P) {
+    const uint32_t K = (P + 63u) & ~63u;
+    if (K > P)
+        for (int l = 0; l < kLayers; l++)
+            cudaMemset2DAsync(m->ac[l] + P, 2 * (size_t)K, 0, 2 * (size_t)(K - P), kNRin[l], m->stream);
+    k_tc_input<<<(P * 64u + 255) / 256, 256, 0, m->stream>>>(dX, P, K, m->ar[0], m->ac[0]);
+}
 
 static int mlp_ensure(rad_mlp* m, uint32_t P) {
     if (m->cap >= P) return RAD_OK;
@@ -237,7 +536,7 @@ extern "C" {
 int rad_mlp_create(int device, uint64_t seed, rad_mlp** out) {
     if (!out) return RAD_E_INVALID;
     *out = nullptr;
-    if (cudaSetDevice(device) != cudaSuccess) return RAD_E_CUDA;
+    if (cudaSetDevice(device) != cudaSuccess || rad::dense_init() != cudaSuccess) return RAD_E_CUDA;
     rad_mlp* m = new rad_mlp();
     m->device = device;
     m->off = offsets();
@@ -245,7 +544,8 @@ int rad_mlp_create(int device, uint64_t seed, rad_mlp** out) {
     if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&m->p, 4 * n) != cudaSuccess || cudaMalloc(&m->p16, 2 * n) != cudaSuccess ||
         cudaMalloc(&m->g, 4 * n) != cudaSuccess || cudaMalloc(&m->m, 4 * n) != cudaSuccess ||
-        cudaMalloc(&m->v, 4 * n) != cudaSuccess || cudaMalloc(&m->loss, 8) != cudaSuccess) {
+        cudaMalloc(&m->v, 4 * n) != cudaSuccess || cudaMalloc(&m->loss, 8) != cudaSuccess ||
+        cudaMalloc(&m->ctr, 8) != cudaSuccess) {
         rad_mlp_destroy(m);
         return RAD_E_NOMEM;
     }
@@ -263,7 +563,14 @@ int rad_mlp_create(int device, uint64_t seed, rad_mlp** out) {
     cudaMemcpy(m->p, h.data(), 4 * n, cudaMemcpyHostToDevice);
     cudaMemset(m->m, 0, 4 * n);
     cudaMemset(m->v, 0, 4 * n);
+    for (int l = 0; l < kLayers; l++)
+        if (cudaMalloc(&m->w16[l], 2 * (size_t)kNRout[l] * kKin[l]) != cudaSuccess ||
+            cudaMalloc(&m->wt16[l], 2 * (size_t)kNRin[l] * kKout[l]) != cudaSuccess) {
+            rad_mlp_destroy(m);
+            return RAD_E_NOMEM;
+        }
     k_to_bf16<<<64, 256, 0, m->stream>>>(m->p, (uint32_t)n, m->p16);
+    tc_refresh(m);
     if (cudaStreamSynchronize(m->stream) != cudaSuccess) {
         rad_mlp_destroy(m);
         return RAD_E_CUDA;
@@ -282,6 +589,12 @@ int rad_mlp_destroy(rad_mlp* m) {
     cudaFree(m->v);
     cudaFree(m->loss);
     cudaFree(m->tgt);
+    tc_free_acts(m);
+    for (int l = 0; l < kLayers; l++) {
+        cudaFree(m->w16[l]);
+        cudaFree(m->wt16[l]);
+    }
+    cudaFree(m->ctr);
     for (int l = 0; l <= kLayers; l++) {
         cudaFree(m->act[l]);
         cudaFree(m->dact[l]);
@@ -292,6 +605,13 @@ int rad_mlp_destroy(rad_mlp* m) {
 }
 
 uint32_t rad_mlp_param_count(void) { return (uint32_t)offsets().total; }
+
+int rad_mlp_set_tensor_cores(rad_mlp* m, int on) {
+    if (!m) return RAD_E_INVALID;
+    if (cudaStreamSynchronize(m->stream) != cudaSuccess) return RAD_E_CUDA;
+    m->tc = on != 0;
+    return RAD_OK;
+}
 
 int rad_mlp_get_params(rad_mlp* m, float* out) {
     if (!m || !out) return RAD_E_INVALID;
@@ -304,16 +624,25 @@ int rad_mlp_set_params(rad_mlp* m, const float* in) {
     cudaStreamSynchronize(m->stream);
     if (cudaMemcpy(m->p, in, 4 * m->off.total, cudaMemcpyHostToDevice) != cudaSuccess) return RAD_E_CUDA;
     k_to_bf16<<<64, 256, 0, m->stream>>>(m->p, (uint32_t)m->off.total, m->p16);
+    tc_refresh(m);
     return cudaStreamSynchronize(m->stream) == cudaSuccess ? RAD_OK : RAD_E_CUDA;
 }
 
 int rad_mlp_predict(rad_mlp* m, const float* X, uint32_t P, float* Y) {
     if (!m || !X || !Y || P == 0) return RAD_E_INVALID;
     int rc = mlp_ensure(m, P);
+    if (!rc && m->tc) rc = tc_ensure(m, P);
     if (rc) return rc;
     cudaMemcpyAsync(m->act[0], X, sizeof(float) * (size_t)P * kIn, cudaMemcpyHostToDevice, m->stream);
-    mlp_forward(m, P);
-    cudaMemcpyAsync(Y, m->act[kLayers], sizeof(float) * (size_t)P * kOut, cudaMemcpyDeviceToHost, m->stream);
+    const float* out = m->act[kLayers];
+    if (m->tc) {
+        tc_stage(m, m->act[0], P);
+        if ((rc = tc_forward(m, P))) return rc;
+        out = m->y;
+    } else {
+        mlp_forward(m, P);
+    }
+    cudaMemcpyAsync(Y, out, sizeof(float) * (size_t)P * kOut, cudaMemcpyDeviceToHost, m->stream);
     return (cudaGetLastError() == cudaSuccess && cudaStreamSynchronize(m->stream) == cudaSuccess) ? RAD_OK : RAD_E_CUDA;
 }
 
@@ -323,8 +652,15 @@ int rad_mlp_gradients(rad_mlp* m, const float* X, const float* T, uint32_t P, fl
     if (rc) return rc;
     cudaMemcpyAsync(m->act[0], X, sizeof(float) * (size_t)P * kIn, cudaMemcpyHostToDevice, m->stream);
     cudaMemcpyAsync(m->tgt, T, sizeof(float) * (size_t)P * kOut, cudaMemcpyHostToDevice, m->stream);
-    mlp_forward(m, P);
-    mlp_backward(m, P);
+    if (m->tc) {
+        if ((rc = tc_ensure(m, P))) return rc;
+        cudaMemsetAsync(m->g, 0, sizeof(float) * m->off.total, m->stream);
+        tc_stage(m, m->act[0], P);
+        if ((rc = tc_forward(m, P)) || (rc = tc_backward(m, P))) return rc;
+    } else {
+        mlp_forward(m, P);
+        mlp_backward(m, P);
+    }
     double l = 0;
     if (grads) cudaMemcpyAsync(grads, m->g, 4 * m->off.total, cudaMemcpyDeviceToHost, m->stream);
     cudaMemcpyAsync(&l, m->loss, 8, cudaMemcpyDeviceToHost, m->stream);
@@ -344,6 +680,7 @@ int rad_mlp_train(rad_mlp* m, const float* X, const float* T, uint32_t P, uint32
         return RAD_E_NOMEM;
     }
     int rc = mlp_ensure(m, batch);
+    if (!rc && m->tc) rc = tc_ensure(m, batch);
     if (rc) {
         cudaFree(dX);
         cudaFree(dT);
@@ -357,7 +694,56 @@ int rad_mlp_train(rad_mlp* m, const float* X, const float* T, uint32_t P, uint32
     cudaEventRecord(e0, m->stream);
     double l = 0;
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-    for (uint32_t ep = 0; ep < epochs; ep++) {
+    if (m->tc && rc == RAD_OK) {
+        // the tensor-core engine: one captured graph per full batch (staging from the device
+        // data set by the batch counter, forward, backward, Adam, BF16 weight copies, counters),
+        // replayed P / batch times per epoch; a last partial batch runs the same kernels directly
+        const uint32_t full = P / batch, rem = P % batch;
+        const uint32_t h_ctr[2] = {m->step, 0u};
+        cudaMemcpyAsync(m->ctr, h_ctr, 8, cudaMemcpyHostToDevice, m->stream);
+        cudaStreamSynchronize(m->stream);
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        if (full > 0) {
+            const uint32_t K = (batch + 63u) & ~63u;
+            bool ok = cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+            if (ok) {
+                if (K > batch)
+                    for (int k = 0; k < kLayers; k++)
+                        cudaMemset2DAsync(m->ac[k] + batch, 2 * (size_t)K, 0, 2 * (size_t)(K - batch), kNRin[k],
+                                          m->stream);
+                k_tc_batch<<<(batch * 64u + 255) / 256, 256, 0, m->stream>>>(dX, dT, batch, K, m->ctr, m->ar[0],
+                                                                             m->ac[0], m->tgt);
+                if (tc_forward(m, batch) || tc_backward(m, batch)) ok = false;
+                k_step_begin<<<1, 1, 0, m->stream>>>(m->ctr);
+                k_adam_dev<<<64, 256, 0, m->stream>>>(m->p, m->g, m->m, m->v, (uint32_t)m->off.total, lr, b1, b2,
+                                                      eps, m->ctr, m->p16);
+                tc_refresh(m);
+                k_step_end<<<1, 1, 0, m->stream>>>(m->ctr, full);
+            }
+            const bool ended = cudaStreamEndCapture(m->stream, &graph) == cudaSuccess;
+            if (!ok || !ended || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) rc = RAD_E_CUDA;
+        }
+        for (uint32_t ep = 0; ep < epochs && rc == RAD_OK; ep++) {
+            for (uint32_t s = 0; s < full && rc == RAD_OK; s++)
+                if (cudaGraphLaunch(exec, m->stream) != cudaSuccess) rc = RAD_E_CUDA;
+            if (rem && rc == RAD_OK) {
+                const size_t at = (size_t)full * batch;
+                cudaMemcpyAsync(m->tgt, dT + at * kOut, sizeof(float) * (size_t)rem * kOut, cudaMemcpyDeviceToDevice,
+                                m->stream);
+                tc_stage(m, dX + at * kIn, rem);
+                if ((rc = tc_forward(m, rem)) || (rc = tc_backward(m, rem))) break;
+                k_step_begin<<<1, 1, 0, m->stream>>>(m->ctr);
+                k_adam_dev<<<64, 256, 0, m->stream>>>(m->p, m->g, m->m, m->v, (uint32_t)m->off.total, lr, b1, b2,
+                                                      eps, m->ctr, m->p16);
+                tc_refresh(m);
+            }
+        }
+        m->step += epochs * (full + (rem ? 1u : 0u));
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
+    for (uint32_t ep = 0; ep < epochs && rc == RAD_OK && !m->tc; ep++) {
         for (uint32_t at = 0; at < P; at += batch) {
             const uint32_t nb = P - at < batch ? P - at : batch;
             cudaMemcpyAsync(m->act[0], dX + (size_t)at * kIn, sizeof(float) * (size_t)nb * kIn,
@@ -374,7 +760,7 @@ int rad_mlp_train(rad_mlp* m, const float* X, const float* T, uint32_t P, uint32
     }
     cudaEventRecord(e1, m->stream);
     cudaMemcpyAsync(&l, m->loss, 8, cudaMemcpyDeviceToHost, m->stream);
-    const bool ok = cudaGetLastError() == cudaSuccess && cudaStreamSynchronize(m->stream) == cudaSuccess;
+    const bool ok = rc == RAD_OK && cudaGetLastError() == cudaSuccess && cudaStreamSynchronize(m->stream) == cudaSuccess;
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);

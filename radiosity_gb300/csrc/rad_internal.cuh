@@ -146,18 +146,31 @@ void launch_argmax(uint32_t n, bool phys, const float4* rad, const float* area, 
 }  // namespace rad
 #include <cuda_bf16.h>
 namespace rad {
+// Epilogue of k_gemm_tc for C = A Bt^T (row = A row, c = Bt row):
+//   mode 0: out[c][row] = scale[row] * acc                       (column-major, + BF16 copy)
+//   mode 1: out[c][row] = resid[c][row] + rho[row].c * (scale * acc)
+//   mode 2: y = max(acc + bias[c], 0): BF16 out16r[row][c] (row-major, ldr) and out16[c][row]
+//   mode 3: out[row][c] = acc + bias[c]                          (row-major FP32, stride R)
+//   mode 4: y = acc if mask[row][c] > 0 else 0 (mask BF16 row-major, ldm): BF16 as mode 2
+//   mode 5: out[row][c] = acc                                    (row-major FP32, stride ldr)
+// Modes 2-5 are the warm-start network's layers (forward, input gradient, weight gradient).
 struct TcEpilogue {
-    int mode;                  // 0: out = scale*acc ; 1: out = resid + rho o (scale*acc)
+    int mode;
     uint32_t n, R;             // rows, output columns
     const float* scale;        // n (may be null: 1)
     const float4* rho;         // n (mode 1)
     const float* resid;        // R x n column-major (mode 1)
-    float* out;                // R x n column-major
+    float* out;                // modes 0, 1: R x n column-major; modes 3, 5: row-major
     __nv_bfloat16* out16;      // R x ld16 (next operand), may be null
     uint32_t ld16;
     uint32_t* err;
     float* partial;            // split-K partial sums, ksplit x R x n (null: one split, fused epilogue)
     uint32_t ksplit;           // K splits (gemm_tc_ksplit); > 1 only with `partial`
+    const float* bias;         // R (modes 2, 3)
+    __nv_bfloat16* out16r;     // row-major BF16 output (modes 2, 4), row stride ldr
+    uint32_t ldr;
+    const __nv_bfloat16* mask; // mode 4, row stride ldm
+    uint32_t ldm;
 };
 void launch_dense_rows(unsigned long long* Fq, uint32_t count, uint32_t n, uint32_t ld, uint32_t first,
                        float* F32, __nv_bfloat16* F16, float* scale, cudaStream_t s);
