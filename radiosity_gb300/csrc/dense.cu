@@ -560,7 +560,9 @@ struct TcShape {
     static constexpr uint32_t kB = NR * kTcBK * 2;
     static constexpr uint32_t kStage = kA + kB;
     static constexpr uint32_t kCols = NR <= 32 ? 32 : (NR <= 64 ? 64 : (NR <= 128 ? 128 : 256));
-    static constexpr uint32_t kSmem = kTcStages * kStage + 1024 + 256;
+    // 1 KB header (mbarriers, TMEM slot), the stage ring, 1 KB of alignment slack
+    static constexpr uint32_t kSmem = kTcStages * kStage + 2048;
+    static constexpr uint32_t smem_for(uint32_t stages) { return stages * kStage + 2048; }
     // instruction descriptor: D f32, A/B bf16, K-major both, N = NR, M = 128
     static constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NR >> 3) << 17) |
                                        ((uint32_t)(kTcM >> 4) << 24);
@@ -624,24 +626,27 @@ __device__ __forceinline__ void net_epilogue(const TcEpilogue& ep, uint32_t row,
     }
 }
 
+// nst: stages of the TMA ring (2..kTcStages); a short K needs fewer, and the smaller shared
+// footprint lets two CTAs share an SM.
 template <int NR>
-__global__ void __launch_bounds__(256, 1) k_gemm_tc(const __grid_constant__ CUtensorMap tmA,
+__global__ void __launch_bounds__(256, 2) k_gemm_tc(const __grid_constant__ CUtensorMap tmA,
                                                     const __grid_constant__ CUtensorMap tmB, uint32_t kblocks,
-                                                    TcEpilogue ep) {
+                                                    uint32_t nst, TcEpilogue ep) {
     using S = TcShape<NR>;
     extern __shared__ uint8_t smem_raw[];
-    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem + kTcStages * S::kStage);
+    uint8_t* hdr = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    uint64_t* full = reinterpret_cast<uint64_t*>(hdr);
     uint64_t* empty = full + kTcStages;
     uint64_t* accum = empty + kTcStages;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+    uint8_t* smem = hdr + 1024;  // stage s at smem + s * kStage (1024-aligned for the 128B swizzle)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t m0 = blockIdx.x * kTcM;
     // split-K: block (x, y) takes K blocks [kb0, kb1) of split y
     const uint32_t nsplit = (ep.partial && ep.ksplit > 1) ? ep.ksplit : 1u, split = blockIdx.y;
     const uint32_t kb0 = split * kblocks / nsplit, kb1 = (split + 1) * kblocks / nsplit;
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kTcStages; s++) {
+        for (uint32_t s = 0; s < nst; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
@@ -660,7 +665,7 @@ __global__ void __launch_bounds__(256, 1) k_gemm_tc(const __grid_constant__ CUte
     const uint32_t taddr = *tmem_slot;
     if (warp == 0 && lane == 0) {
         for (uint32_t kb = kb0; kb < kb1; kb++) {
-            const uint32_t s = (kb - kb0) % kTcStages, round = (kb - kb0) / kTcStages;
+            const uint32_t s = (kb - kb0) % nst, round = (kb - kb0) / nst;
             if (!mbar_wait(&empty[s], (round & 1u) ^ 1u, ep.err)) break;
             mbar_expect_tx(&full[s], S::kStage);
             tma_load_2d(smem + s * S::kStage, &tmA, (int)(kb * kTcBK), (int)m0, &full[s]);
@@ -669,7 +674,7 @@ __global__ void __launch_bounds__(256, 1) k_gemm_tc(const __grid_constant__ CUte
     } else if (warp == 1 && lane == 0) {
         bool ok = true;
         for (uint32_t kb = kb0; kb < kb1; kb++) {
-            const uint32_t s = (kb - kb0) % kTcStages, round = (kb - kb0) / kTcStages;
+            const uint32_t s = (kb - kb0) % nst, round = (kb - kb0) / nst;
             if (!mbar_wait(&full[s], round & 1u, ep.err)) {
                 ok = false;
                 break;
@@ -822,6 +827,25 @@ __global__ void k_tc_finalize(TcEpilogue ep) {
     }
 }
 
+// Split-K epilogue for many splits (the network's weight gradients): a warp per element, lane
+// l adding splits l, l + 32, ... in order, then a fixed shuffle tree, so the sum is the same
+// on every run.
+__global__ void k_tc_finalize_wide(TcEpilogue ep) {
+    const size_t total = (size_t)ep.R * ep.n;
+    const uint32_t lane = threadIdx.x & 31;
+    const size_t warps = (size_t)gridDim.x * (blockDim.x >> 5);
+    const size_t stride = (size_t)ep.R * ep.n;
+    for (size_t e = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); e < total; e += warps) {
+        const uint32_t c = (uint32_t)(e / ep.n), row = (uint32_t)(e % ep.n);
+        const size_t at = (size_t)c * ep.n + row;
+        float acc = 0.f;
+        for (uint32_t sp = lane; sp < ep.ksplit; sp += 32) acc += ep.partial[sp * stride + at];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) net_store(ep, row, c, acc);
+    }
+}
+
 // K splits for n rows and R right-hand sides: the count (1..8, at least 8 K blocks each)
 // that minimises the bytes moved per row, with the F reads (2 ld bytes) divided by the
 // share of the 152 SMs the last wave keeps busy, plus the partial sums written and read
@@ -892,8 +916,11 @@ static int launch_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv
     if (attr != cudaSuccess) return -2;
     const uint32_t kblocks = ld / kTcBK;
     const uint32_t nsplit = (ep.partial && ep.ksplit > 1) ? ep.ksplit : 1u;
-    k_gemm_tc<NR><<<dim3((n + kTcM - 1) / kTcM, nsplit), 256, S::kSmem, s>>>(ma, mb, kblocks, ep);
-    if (nsplit > 1) k_tc_finalize<<<152 * 8, 256, 0, s>>>(ep);
+    const uint32_t per_split = (kblocks + nsplit - 1) / nsplit;  // K blocks of the longest split
+    const uint32_t nst = per_split >= (uint32_t)kTcStages ? (uint32_t)kTcStages : (per_split < 2u ? 2u : per_split);
+    k_gemm_tc<NR><<<dim3((n + kTcM - 1) / kTcM, nsplit), 256, S::smem_for(nst), s>>>(ma, mb, kblocks, nst, ep);
+    if (nsplit >= 32 && ep.mode >= 2) k_tc_finalize_wide<<<152 * 8, 256, 0, s>>>(ep);
+    else if (nsplit > 1) k_tc_finalize<<<152 * 8, 256, 0, s>>>(ep);
     return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 

@@ -262,31 +262,47 @@ __global__ void k_tc_weights(const float* __restrict__ p, TcWeights tw) {
     }
 }
 
+// One row of X (32 FP32) -> A_0: BF16 row-major [r][0..32) (columns 32..63 stay zero) as four
+// 16-byte stores, and column-major [k][r] (consecutive rows in consecutive lanes: coalesced).
+__device__ __forceinline__ void tc_input_row(const float* __restrict__ x, uint32_t r, uint32_t K,
+                                             __nv_bfloat16* __restrict__ ar, __nv_bfloat16* __restrict__ ac) {
+    const float4* x4 = reinterpret_cast<const float4*>(x);
+    uint32_t packed[16];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const float4 f = x4[q];
+        const __nv_bfloat162 h0 = __floats2bfloat162_rn(f.x, f.y), h1 = __floats2bfloat162_rn(f.z, f.w);
+        packed[2 * q] = *reinterpret_cast<const uint32_t*>(&h0);
+        packed[2 * q + 1] = *reinterpret_cast<const uint32_t*>(&h1);
+        ac[(size_t)(4 * q) * K + r] = h0.x;
+        ac[(size_t)(4 * q + 1) * K + r] = h0.y;
+        ac[(size_t)(4 * q + 2) * K + r] = h1.x;
+        ac[(size_t)(4 * q + 3) * K + r] = h1.y;
+    }
+    uint4* dst = reinterpret_cast<uint4*>(ar + (size_t)r * 64);
+#pragma unroll
+    for (int q = 0; q < 4; q++) dst[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
+}
+
 // The batch ctr[1] of a data set on the device: rows [ctr[1] * P, +P) of X -> A_0 (as
-// k_tc_input) and of T -> tgt.
+// k_tc_input) and of T -> tgt; thread per row.
 __global__ void k_tc_batch(const float* __restrict__ X, const float* __restrict__ T, uint32_t P, uint32_t K,
                            const uint32_t* __restrict__ ctr, __nv_bfloat16* __restrict__ ar,
                            __nv_bfloat16* __restrict__ ac, float* __restrict__ tgt) {
-    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= P * 64u) return;
-    const uint32_t r = e / 64u, k = e % 64u;
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= P) return;
     const size_t src = (size_t)ctr[1] * P + r;
-    const __nv_bfloat16 h = __float2bfloat16_rn(k < (uint32_t)kIn ? X[src * kIn + k] : 0.f);
-    ar[e] = h;
-    if (k < (uint32_t)kIn) ac[(size_t)k * K + r] = h;
-    if (k < (uint32_t)kOut) tgt[(size_t)r * kOut + k] = T[src * kOut + k];
+    tc_input_row(X + src * kIn, r, K, ar, ac);
+#pragma unroll
+    for (int k = 0; k < kOut; k++) tgt[(size_t)r * kOut + k] = T[src * kOut + k];
 }
 
 // X (P x 32 FP32) -> A_0 row-major [P][64] and column-major [32][K] in BF16 (K = pad64(P),
-// the row pitch of every column-major buffer for this batch).
+// the row pitch of every column-major buffer for this batch); thread per row.
 __global__ void k_tc_input(const float* __restrict__ X, uint32_t P, uint32_t K, __nv_bfloat16* __restrict__ ar,
                            __nv_bfloat16* __restrict__ ac) {
-    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= P * 64u) return;
-    const uint32_t r = e / 64u, k = e % 64u;
-    const __nv_bfloat16 h = __float2bfloat16_rn(k < (uint32_t)kIn ? X[(size_t)r * kIn + k] : 0.f);
-    ar[e] = h;
-    if (k < (uint32_t)kIn) ac[(size_t)k * K + r] = h;
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < P) tc_input_row(X + (size_t)r * kIn, r, K, ar, ac);
 }
 
 // MSE: dY = 2 (Y - T) / (3P) in BF16 (row-major [P][64], column-major [3][K]); loss sum.
@@ -474,7 +490,7 @@ static void tc_stage(rad_mlp* m, const float* dX, uint32_t P) {
     if (K > P)
         for (int l = 0; l < kLayers; l++)
             cudaMemset2DAsync(m->ac[l] + P, 2 * (size_t)K, 0, 2 * (size_t)(K - P), kNRin[l], m->stream);
-    k_tc_input<<<(P * 64u + 255) / 256, 256, 0, m->stream>>>(dX, P, K, m->ar[0], m->ac[0]);
+    k_tc_input<<<(P + 127) / 128, 128, 0, m->stream>>>(dX, P, K, m->ar[0], m->ac[0]);
 }
 
 static int mlp_ensure(rad_mlp* m, uint32_t P) {
@@ -712,8 +728,8 @@ int rad_mlp_train(rad_mlp* m, const float* X, const float* T, uint32_t P, uint32
                     for (int k = 0; k < kLayers; k++)
                         cudaMemset2DAsync(m->ac[k] + batch, 2 * (size_t)K, 0, 2 * (size_t)(K - batch), kNRin[k],
                                           m->stream);
-                k_tc_batch<<<(batch * 64u + 255) / 256, 256, 0, m->stream>>>(dX, dT, batch, K, m->ctr, m->ar[0],
-                                                                             m->ac[0], m->tgt);
+                k_tc_batch<<<(batch + 127) / 128, 128, 0, m->stream>>>(dX, dT, batch, K, m->ctr, m->ar[0],
+                                                                       m->ac[0], m->tgt);
                 if (tc_forward(m, batch) || tc_backward(m, batch)) ok = false;
                 k_step_begin<<<1, 1, 0, m->stream>>>(m->ctr);
                 k_adam_dev<<<64, 256, 0, m->stream>>>(m->p, m->g, m->m, m->v, (uint32_t)m->off.total, lr, b1, b2,
