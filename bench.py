@@ -71,8 +71,8 @@ def parse():
     p.add_argument("--train-patches", default="5000,50000", help="learned: training patch range (log-uniform)")
     p.add_argument("--train-sample", type=int, default=2048, help="learned: patches kept per training scene")
     p.add_argument("--train-epochs", type=int, default=50, help="learned: training epochs")
-    p.add_argument("--train-batch", type=int, default=4096, help="warm-start network: rows per Adam step")
-    p.add_argument("--train-lr", type=float, default=2e-3, help="warm-start network: Adam learning rate")
+    p.add_argument("--train-batch", type=int, default=16384, help="warm-start network: rows per Adam step")
+    p.add_argument("--train-lr", type=float, default=3e-3, help="warm-start network: Adam learning rate")
     p.add_argument("--eval-scenes", type=int, default=100, help="learned: held-out room scenes")
     p.add_argument("--eval-patches", type=int, default=50000, help="learned: patch target of a held-out room")
     p.add_argument("--learned-w", type=int, default=128, help="learned: hemicube side of the training captures")
