@@ -157,21 +157,37 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(k: int):
-    """DRAM bytes per raster launch from the committed ncu summary (per hemicube x K)."""
+RASTER_PROFILE = os.path.join("profiles", "k_raster_room50k_w512.json")
+
+
+def raster_profile():
+    """The committed ncu summary of the raster kernel on this workload (profiles/), with the
+    commands that produced it: DRAM traffic per hemicube (one-pass metrics at K=32) and the
+    SM-side utilisation of the full section set (K=8).  None when the file is absent."""
     try:
-        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
-            d = json.load(f)
-        return float(d["raster_dram_bytes_per_hemicube"]) * k
+        with open(os.path.join(ROOT, RASTER_PROFILE)) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+def ncu_traffic(k: int):
+    """DRAM bytes per raster launch: the profile's per-hemicube figure x K."""
+    prof = raster_profile()
+    try:
+        return float(prof["traffic"]["dram_bytes_per_hemicube"]) * k
     except Exception:
         return None
 
 
 def sm_side_ncu():
-    """k_raster's SM-side figures from profiles/k_raster_k_setup_full_room50k_w512_k8.md."""
-    return {"source": "profiles/k_raster_k_setup_full_room50k_w512_k8.md (ncu --set full, K=8)",
-            "issue_slots_busy_frac": 0.536, "shared_pipe_frac": 0.594, "sm_throughput_frac": 0.382,
-            "active_lanes_per_warp_instruction": 24.6, "dram_throughput_frac": 0.022}
+    """k_raster's SM-side figures and its bounding SM unit, read from the committed profile."""
+    prof = raster_profile()
+    if not prof or "sm_side" not in prof:
+        return None
+    out = dict(prof["sm_side"])
+    out["source"] = RASTER_PROFILE + " (" + prof["sm_side"].get("capture", "ncu --set full") + ")"
+    return out
 
 
 def cpu_baseline(sc, W, K, seconds):

@@ -428,20 +428,38 @@ __global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* _
         if (!behind)
             for (int f = 0; f < 5; f++) {
                 // the z and w rows first: all four corners outside the near plane
-                // (z + w < 0) reject the face without the x and y rows; the rows are the
-                // same float expressions as face_corners', so the mask is unchanged
+                // (z + w < 0) reject the face without the x and y rows.  The rows are the
+                // same float expressions as face_corners', and the tests below are its
+                // tests on the same values, so the mask is unchanged.
                 const float* mm = s_mvp + f * 16;
+                float cz[4], cw[4];
                 bool near_out = true;
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
                     const float x = q[3 * k], y = q[3 * k + 1], z = q[3 * k + 2];
-                    const float cz = ((mm[2] * x + mm[6] * y) + mm[10] * z) + mm[14];
-                    const float cw = ((mm[3] * x + mm[7] * y) + mm[11] * z) + mm[15];
-                    if (!(cz + cw < 0)) near_out = false;
+                    cz[k] = ((mm[2] * x + mm[6] * y) + mm[10] * z) + mm[14];
+                    cw[k] = ((mm[3] * x + mm[7] * y) + mm[11] * z) + mm[15];
+                    if (!(cz[k] + cw[k] < 0)) near_out = false;
                 }
                 if (near_out) continue;
-                float4 cv[4];
-                if (face_corners(q, mm, f, cv)) mask |= 1u << f;
+                uint32_t out_any = 0x3F, in_half = 0;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const float x = q[3 * k], y = q[3 * k + 1], z = q[3 * k + 2];
+                    const float cx = ((mm[0] * x + mm[4] * y) + mm[8] * z) + mm[12];
+                    const float cy = ((mm[1] * x + mm[5] * y) + mm[9] * z) + mm[13];
+                    uint32_t o = 0;
+                    if (cz[k] + cw[k] < 0) o |= 1;
+                    if (cw[k] - cz[k] < 0) o |= 2;
+                    if (cx > cw[k]) o |= 4;
+                    if (cx < -cw[k]) o |= 8;
+                    if (cy > cw[k]) o |= 16;
+                    if (cy < -cw[k]) o |= 32;
+                    out_any &= o;
+                    const bool keep = f == 0 ? cy < 0 : (f == 1 ? cy > 0 : (f == 2 ? cx > 0 : (f == 3 ? cx < 0 : true)));
+                    if (keep) in_half = 1;
+                }
+                if (!out_any && in_half) mask |= 1u << f;
             }
     }
     // 2. compaction
