@@ -363,9 +363,13 @@ def run_ours(args):
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_kind": peak_kind, "traffic": ncu_traffic(K),
                      "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_ms": raster_ms,
-                     # the raster is SM-bound, not DRAM-bound: its SM-side utilisation from the
-                     # committed full-section ncu capture (K=8 case of the same scene)
-                     "sm_side_ncu": sm_side_ncu()},
+                     # the raster is SM-bound, not DRAM-bound: its SM-side utilisation and the
+                     # bounding SM unit from the committed full-section ncu capture (K=8 case
+                     # of the same scene, profiles/k_raster_room50k_w512.json)
+                     "sm_side_ncu": sm_side_ncu(),
+                     "sm_bound": (lambda p: None if not p else {"unit": p["bounding_unit"],
+                                                                 "frac": p["bounding_unit_frac"],
+                                                                 "source": RASTER_PROFILE})(sm_side_ncu())},
         "stage_ms_per_step": {k: v / batches for k, v in stage_ms.items()},
         "raster_counters_per_hemicube": counters,
         "gpu_launches": int(launches_per_step * st.shots_done),
