@@ -498,7 +498,7 @@ def train_warm_start(args, scenes_n: int = 48, epochs: int = 200, patches=(2000,
 
     t0 = time.perf_counter()
     X, T = learned.training_set(scenes_n, seed=args.seed, patches=patches, W=W, kinds=kinds, sample=sample,
-                                workers=workers)
+                                workers=workers, form=learned.FORM)
     gen_s = time.perf_counter() - t0
     order = np.random.default_rng(args.seed).permutation(X.shape[0])  # batches mix scenes
     X, T = np.ascontiguousarray(X[order]), np.ascontiguousarray(T[order])
@@ -510,7 +510,7 @@ def train_warm_start(args, scenes_n: int = 48, epochs: int = 200, patches=(2000,
     return m, {"scenes": scenes_n, "kinds": list(kinds), "patch_range": list(patches), "W": W,
                "samples": int(X.shape[0]), "sample_per_scene": sample, "epochs": epochs, "batch": batch, "lr": lr,
                "final_loss": loss, "train_ms": train_ms, "train_tflops": flop / (train_ms * 1e9),
-               "engine": "tcgen05 BF16 GEMMs", "data_gen_s": gen_s}
+               "engine": "tcgen05 BF16 GEMMs", "data_gen_s": gen_s, "form": learned.FORM}
 
 
 def learned_headline(args):
@@ -546,7 +546,8 @@ def run_learned(args):
                                    workers=args.gen_workers)
     if args.save_weights:
         learned.save_network(m, args.save_weights, {"training": training, "features": "learned.features",
-                                                   "network": "32-128x4-3 ReLU, BF16 weights"})
+                                                   "network": "32-128x4-3 ReLU, BF16 weights",
+                                                   "form": learned.FORM})
     names = ("emission", "direct", "learned")
     rows, caps, npat = [], [], []
     t0 = time.perf_counter()
@@ -599,12 +600,13 @@ def headline(args, m, sc):
     """Time to residual <= 1e-4 on one large scene: learned warm start + BF16 gather (dense capture
     included) against the plain FP32 progressive shooter, both at W=args.w on this GPU.
 
-    Each method is stopped by the relative L2 residual of its own discrete system on the captured
-    FP32 rows: the gather solves B = E + rho o (F B); the shooter, which spreads power with the
-    reciprocity form F_ji = F_ij A_i / A_j, solves B = E + rho o (F^T (A o B)) / A.  The two fixed
-    points differ by the hemicube reciprocity error (reported).  The shooter runs in segments of
+    Both methods solve the same discrete system and stop on its relative L2 residual on the
+    captured FP32 rows: the shooter spreads power with the reciprocity form F_ji = F_ij A_i / A_j,
+    so its fixed point is B = E + rho o (F^T (A o B)) / A, and the gather runs in the shoot form
+    (RAD_DENSE_SHOOT_FORM), which iterates on that same system.  The shooter runs in segments of
     16 batches with its total radiosity (shot + unshot) checked after each (untimed); its own
-    unshot-power rule is recorded beside it.  Final answers are checked in FP64 on the host."""
+    unshot-power rule is recorded beside it.  Final answers are checked in FP64 on the host, and
+    their relative L2 difference is reported."""
     import radiosity_gb300 as R
     from radiosity_gb300 import learned
 
@@ -616,7 +618,7 @@ def headline(args, m, sc):
     g = R.Solver(hemicube_side=W, hemicubes_count=args.k, mode=R.MODE_PHYS)
     g.upload(sc["vertices"], sc["color"], sc["radiosity"], sc["illumination"], reflectance=sc["reflectance"])
     tune = g.autotune()
-    cap_ms = g.dense_capture(keep_fp32=True)
+    cap_ms = g.dense_capture(keep_fp32=True, form=learned.FORM)
     t1 = time.perf_counter()
     d = learned.direct_light(g, E)
     guess = learned.warm_start(m, sc, d)
@@ -655,20 +657,20 @@ def headline(args, m, sc):
     area = 0.5 * np.linalg.norm(np.cross(v[:, 0] - v[:, 2], v[:, 1] - v[:, 3]), axis=1)
     Bg = B.T.astype(np.float64)
     FBp = np.zeros((n, 3))
-    FBg = np.zeros((n, 3))
     FTp = np.zeros((n, 3))
+    FTg = np.zeros((n, 3))
     for r0 in range(0, n, 4096):
         F, _, _ = g.dense_rows(r0, min(4096, n - r0))
         Fd = F.astype(np.float64)
         r1 = r0 + len(F)
         FBp[r0:r1] = Fd @ Bp
-        FBg[r0:r1] = Fd @ Bg
         FTp += Fd.T @ (area[r0:r1, None] * Bp[r0:r1])
+        FTg += Fd.T @ (area[r0:r1, None] * Bg[r0:r1])
     g.close()
     nE = np.linalg.norm(E64)
-    res_p64 = float(np.linalg.norm(E64 + rho * FTp / area[:, None] - Bp) / nE)  # shooter, own system
-    res_p_gather = float(np.linalg.norm(E64 + rho * FBp - Bp) / nE)  # shooter answer, gather system
-    res_g64 = float(np.linalg.norm(E64 + rho * FBg - Bg) / nE)
+    res_p64 = float(np.linalg.norm(E64 + rho * FTp / area[:, None] - Bp) / nE)  # shooter
+    res_p_gather = float(np.linalg.norm(E64 + rho * FBp - Bp) / nE)  # shooter answer, B = E + rho o (F B)
+    res_g64 = float(np.linalg.norm(E64 + rho * FTg / area[:, None] - Bg) / nE)  # gather, same system
     rel_diff = float(np.linalg.norm(Bg - Bp) / np.linalg.norm(Bg))
     learned_s = (cap_ms + st.device_ms) / 1000 + (t2 - t1)
     return {"patches": n, "W": W, "K": int(args.k), "tol": tol,
@@ -679,7 +681,7 @@ def headline(args, m, sc):
             "learned_gather": {"capture_s": cap_ms / 1000, "predict_host_s": t2 - t1,
                                "solve_s": st.device_ms / 1000, "outer": st.outer, "sweeps": st.sweeps,
                                "initial_residual": st.initial_residual, "residual": st.residual,
-                               "fp64_residual": res_g64, "total_s": learned_s},
+                               "fp64_residual": res_g64, "total_s": learned_s, "form": learned.FORM},
             "gather_from_emission": {"solve_s": st0.device_ms / 1000, "outer": st0.outer, "sweeps": st0.sweeps,
                                      "initial_residual": st0.initial_residual},
             "answers_rel_l2_difference": rel_diff,
@@ -696,7 +698,9 @@ def warm_start_network(args):
     got = learned.load_network()
     if got is not None:
         m, meta = got
-        return m, dict(meta.get("training", {}), source="shipped network " + os.path.relpath(learned.WEIGHTS, ROOT))
+        if meta.get("training", {}).get("form") == learned.FORM:
+            return m, dict(meta["training"], source="shipped network " + os.path.relpath(learned.WEIGHTS, ROOT))
+        m.close()
     m, training = train_warm_start(args)
     return m, dict(training, source="trained in this run")
 
@@ -712,8 +716,9 @@ def run_uneven(args):
     """Uneven batch: 256 Cornell-variant scenes, patches log-uniform in [500, 8000], 1-3 lights, W=128.
 
     Both arms run under one captured CUDA graph, and both stop each scene by the same rule: the
-    relative residual max_c ||r_c|| / ||E_c|| of the scene's own discrete system <= tol, on its
-    captured FP32 form-factor rows.
+    relative residual max_c ||r_c|| / ||E_c|| of the shooter's discrete system
+    B = E + rho o (F^T (A o B)) / A <= tol, on the scene's captured FP32 form-factor rows (the
+    gather runs in the shoot form, so both arms solve that system).
       * Plain FP32 shooter (rad_multi): one replay advances every scene by one batch.  The graph
         is replayed in segments of 16 and each open scene's own-system residual (the reciprocity
         form of the shoot update) is checked after each segment, untimed; a scene's time is the
@@ -750,7 +755,7 @@ def run_uneven(args):
     # ---- plain shooter under one graph (device stop rule off: the residual rule stops it)
     solvers = [make(sc, K, tolerance=1e-12, **shape) for sc, K in zip(scs, ks)]
     for s in solvers:  # the FP32 rows for the residual rule (untimed)
-        s.dense_capture(keep_fp32=True)
+        s.dense_capture(keep_fp32=True, form=learned.FORM)
     t_done = np.zeros(n_scenes)
     reps_done = np.zeros(n_scenes, np.int64)
     res_plain = np.ones(n_scenes)
@@ -785,19 +790,21 @@ def run_uneven(args):
     ctxs = [make(sc, 16, **shape) for sc in scs]
     try:
         t0 = time.perf_counter()
-        mg = R.MultiGather(ctxs, mlp=m, tol=tol, max_outer=100, sweeps=4)
+        mg = R.MultiGather(ctxs, mlp=m, tol=tol, max_outer=100, sweeps=4, form=learned.FORM)
         build_s = time.perf_counter() - t0
         t0 = time.perf_counter()
         out = mg.run()
         wall = time.perf_counter() - t0
         fp64 = []
-        for i in range(4):  # FP64 residual of the gather system on the FP32 rows
+        for i in range(4):  # FP64 residual of the shooter's system on the FP32 rows
             n = sizes[i]
             F, _, _ = ctxs[i].dense_rows(0, n)
             B = mg.result(i).T.astype(np.float64)
             E64 = Es[i].T.astype(np.float64)
             rho = scs[i]["reflectance"].reshape(n, 3).astype(np.float64)
-            fp64.append(_rel_residual((E64 + rho * (F.astype(np.float64) @ B) - B).T, Es[i]))
+            a = learned.patch_geometry(scs[i]["vertices"])[2][:, None]
+            FT = F.astype(np.float64).T @ (a * B)
+            fp64.append(_rel_residual((E64 + rho * FT / a - B).T, Es[i]))
         mg.close()
     finally:
         for c in ctxs:

@@ -165,6 +165,15 @@ int rad_autotune(rad_ctx* ctx, uint32_t flags, rad_tuning* out);
  * BF16 Jacobi sweeps of the correction on tcgen05 tensor cores (FP32 accumulation),
  * FP64 norms.  rho is the scene's reflectance (PHYS mode). */
 #define RAD_DENSE_FP32 1u /* also keep FP32 rows: needed by rad_gather_solve */
+/* Shoot form: solve the fixed point of the progressive shooter instead,
+ *     B_i = E_i + rho_i (sum_j F_ji A_j B_j) / A_i,
+ * whose transfer j -> i is F_ji A_j / A_i: the reciprocity form the shoot update uses
+ * (source/Main.cpp:1268-1276 with the area ratio of the PHYS rule).  The capture also keeps
+ * the transposed rows (BF16, and FP32 with RAD_DENSE_FP32) and the area weights; the gather
+ * then converges to the plain shooter's answer.  rad_gather_solve, rad_gather_residual and
+ * the multi-scene graph use the form of the last capture; rad_dense_rows still returns rows
+ * of F.  PHYS mode only. */
+#define RAD_DENSE_SHOOT_FORM 2u
 
 /* Captures every row of F (N hemicubes).  device_ms may be NULL. */
 int rad_dense_capture(rad_ctx* ctx, uint32_t flags, double* device_ms);
@@ -193,7 +202,8 @@ int rad_gather_solve(rad_ctx* ctx, const float* emission, uint32_t R, const floa
                      uint32_t max_outer, uint32_t sweeps, float* radiosity, rad_gather_stats* stats);
 
 /* r = E + rho o (F B) - B with the FP32 rows (column-major N x R host arrays); with B = E
- * this is the first-shot direct light rho o (F E). */
+ * this is the first-shot direct light rho o (F E).  In the shoot form F B is replaced by
+ * (sum_j F_ji A_j B_j) / A_i, as in rad_shoot_residual. */
 int rad_gather_residual(rad_ctx* ctx, const float* emission, uint32_t R, const float* radiosity, float* residual);
 
 /* Residual of the system the progressive shooter solves, r_j = E_j + rho_j (sum_i F_ij A_i B_i)
@@ -256,7 +266,8 @@ int rad_multi_destroy(rad_multi* m);
 /* ---- Many scenes solved by learned warm start + BF16 gather under one CUDA graph ----------
  * No counterpart in the reference.  Each context (PHYS mode, scene uploaded; its unshot
  * energy is the emission E) is a branch of one captured graph: dense capture of its form
- * factors, E and its norms, the first-shot direct light rho o (F E), the network's 32 features
+ * factors (flags: 0 or RAD_DENSE_SHOOT_FORM, the system every branch solves), E and its
+ * norms, the first-shot direct light rho o (F E), the network's 32 features
  * per patch and its guess (or, with mlp NULL, the guess E), the guess's residual, then the
  * refinements of rad_gather_solve (`sweeps` BF16 tcgen05 sweeps, update, FP32 residual with
  * FP64 norms) in a conditional loop that the device ends once the scene's relative residual
@@ -266,7 +277,8 @@ int rad_multi_destroy(rad_multi* m);
  * (rad_dense_rows) after a run. */
 typedef struct rad_multi_gather rad_multi_gather;
 int rad_multi_gather_create(rad_ctx* const* ctxs, uint32_t count, const rad_mlp* mlp, const double* feature_dirs,
-                            double tol, uint32_t max_outer, uint32_t sweeps, rad_multi_gather** out);
+                            double tol, uint32_t max_outer, uint32_t sweeps, uint32_t flags,
+                            rad_multi_gather** out);
 /* One graph launch: every scene solved.  Per scene (arrays of count, any may be NULL): the
  * device ms from the graph's start to its final check, residual evaluations, final and
  * initial relative residual, status (1 converged, 2 stopped by max_outer, 3 non-finite);

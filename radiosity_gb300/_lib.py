@@ -27,6 +27,8 @@ RAD_E_NOALLOC_LIMIT = -7
 RAD_E_NUMERIC = -8
 NOALLOC_MAX_SUMS = 1 << 20
 MODE_REF, MODE_PHYS = 0, 1
+DENSE_FP32, DENSE_SHOOT_FORM = 1, 2
+FORMS = {"gather": 0, "shoot": DENSE_SHOOT_FORM}
 
 # Every symbol include/radiosity.h declares.
 EXPORTS = [
@@ -157,7 +159,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rad_multi_shoot.argtypes = [vp, ctypes.c_uint32, vp, vp, P(ctypes.c_uint32), P(ctypes.c_double)]
     L.rad_multi_destroy.argtypes = [vp]
     L.rad_multi_gather_create.argtypes = [P(vp), ctypes.c_uint32, vp, vp, ctypes.c_double, ctypes.c_uint32,
-                                          ctypes.c_uint32, P(vp)]
+                                          ctypes.c_uint32, ctypes.c_uint32, P(vp)]
     L.rad_multi_gather_run.argtypes = [vp, P(ctypes.c_double), vp, vp, vp, vp, vp]
     L.rad_multi_gather_result.argtypes = [vp, ctypes.c_uint32, _f32p]
     L.rad_multi_gather_destroy.argtypes = [vp]
@@ -490,10 +492,13 @@ class Solver:
         self.cfg.hemicubes_count = t.hemicubes_count
         return t
 
-    def dense_capture(self, keep_fp32: bool = True) -> float:
-        """rad_dense_capture: every form-factor row; returns device ms."""
+    def dense_capture(self, keep_fp32: bool = True, form: str = "gather") -> float:
+        """rad_dense_capture: every form-factor row; returns device ms.  form "gather" solves
+        B = E + rho o (F B); "shoot" (RAD_DENSE_SHOOT_FORM) the progressive shooter's fixed point
+        B = E + rho o (F^T (A o B)) / A."""
         ms = ctypes.c_double()
-        self._check(self.L.rad_dense_capture(self.h, 1 if keep_fp32 else 0, ctypes.byref(ms)), "rad_dense_capture")
+        flags = (DENSE_FP32 if keep_fp32 else 0) | FORMS[form]
+        self._check(self.L.rad_dense_capture(self.h, flags, ctypes.byref(ms)), "rad_dense_capture")
         return ms.value
 
     def dense_rows(self, first: int, count: int):
@@ -515,7 +520,8 @@ class Solver:
         return out, st
 
     def gather_residual(self, emission, radiosity):
-        """rad_gather_residual: r = E + rho o (F B) - B (R x N arrays)."""
+        """rad_gather_residual: r = E + rho o (M B) - B (R x N arrays), M the captured form's
+        operator (F, or F^T with the area weights in the shoot form)."""
         E = np.ascontiguousarray(emission, np.float32)
         B = np.ascontiguousarray(radiosity, np.float32)
         r = np.zeros_like(E)
@@ -689,7 +695,8 @@ class MultiGather:
     captured CUDA graph: dense capture, features, network guess and the refinement loop (a
     conditional node) all run on the device; each scene stops at its own tolerance."""
 
-    def __init__(self, solvers, mlp=None, tol: float = 1e-4, max_outer: int = 100, sweeps: int = 4):
+    def __init__(self, solvers, mlp=None, tol: float = 1e-4, max_outer: int = 100, sweeps: int = 4,
+                 form: str = "gather"):
         self.L = load()
         self.solvers = list(solvers)
         arr = (ctypes.c_void_p * len(self.solvers))(*[s.h.value for s in self.solvers])
@@ -701,7 +708,7 @@ class MultiGather:
             dirs = self._dirs.ctypes.data_as(ctypes.c_void_p)
         h = ctypes.c_void_p()
         rc = self.L.rad_multi_gather_create(arr, len(self.solvers), mlp.h if mlp is not None else None, dirs, tol,
-                                            max_outer, sweeps, ctypes.byref(h))
+                                            max_outer, sweeps, FORMS[form], ctypes.byref(h))
         if rc:
             raise RadError(rc, "rad_multi_gather_create")
         self.h = h

@@ -77,6 +77,8 @@ void launch_dense_rows(unsigned long long* Fq, uint32_t count, uint32_t n, uint3
 
 // ---------------------------------------------------------------------------
 // FP32 residual GEMM: r[c][i] = E[c][i] + rho_i[c%3] * sum_j F[i][j] X[c][j] - X[c][i]
+// (with weights w and inv_a: the sum is over F[i][j] w_j X[c][j] and is multiplied by inv_a_i;
+// the shoot form passes the transposed rows, w = A and inv_a = 1 / A)
 // 128 (rows) x 64 (columns) tiles, 16-deep k slabs staged in shared memory (the next
 // slab's global loads are issued before the current slab's FMAs), 8x4 outputs per thread.
 // Every 64 k the FP32 partial sums are added to a (hi, lo) pair with Knuth's TwoSum, so the
@@ -90,7 +92,8 @@ constexpr int kRBM = 128, kRBN = 64, kRBK = 16, kRComp = 4;  // kRComp slabs bet
 __global__ void __launch_bounds__(256) k_sgemm_resid(const float* __restrict__ F, uint32_t n, uint32_t ld,
                                                      const float* __restrict__ X, const float* __restrict__ E,
                                                      const float4* __restrict__ rho, uint32_t R, float* r,
-                                                     double* nrm) {
+                                                     double* nrm, const float* __restrict__ w,
+                                                     const float* __restrict__ inv_a) {
     __shared__ __align__(16) float As[kRBK][kRBM + 4];  // As[k][i]
     __shared__ __align__(16) float Bs[kRBK][kRBN + 4];  // Bs[k][c]
     const uint32_t i0 = blockIdx.x * kRBM, c0 = blockIdx.y * kRBN;
@@ -108,7 +111,7 @@ __global__ void __launch_bounds__(256) k_sgemm_resid(const float* __restrict__ F
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             const uint32_t gk = k0 + bk + j;
-            rb[j] = (gc < R && gk < n) ? X[(size_t)gc * n + gk] : 0.f;
+            rb[j] = (gc < R && gk < n) ? X[(size_t)gc * n + gk] * (w ? w[gk] : 1.0f) : 0.f;
         }
     };
     float acc[8][4], hi[8][4], lo[8][4];
@@ -164,7 +167,8 @@ __global__ void __launch_bounds__(256) k_sgemm_resid(const float* __restrict__ F
                 if (i >= n) continue;
                 const float4 rh = rho[i];
                 const float rr = ch == 0 ? rh.x : (ch == 1 ? rh.y : rh.z);
-                const float v = E[(size_t)c * n + i] + rr * (hi[p][q] + lo[p][q]) - X[(size_t)c * n + i];
+                const float sum = (hi[p][q] + lo[p][q]) * (inv_a ? inv_a[i] : 1.0f);
+                const float v = E[(size_t)c * n + i] + rr * sum - X[(size_t)c * n + i];
                 r[(size_t)c * n + i] = v;
                 part += (double)v * (double)v;
             }
@@ -264,11 +268,13 @@ constexpr int kNStageBytes = kNRows * kNCols * 4;  // 32 KB
 constexpr int kNSmem = kNStages * kNStageBytes + 2 * kNStages * 8;
 
 // Xp[c][k] = X[c][k] for c < R, k < n, else 0; Xp has kNR rows of pitch ld.
-__global__ void k_pad_rhs(const float* __restrict__ X, uint32_t n, uint32_t R, uint32_t ld, float* __restrict__ Xp) {
+// With weights w: Xp[c][k] = w[k] * X[c][k].
+__global__ void k_pad_rhs(const float* __restrict__ X, uint32_t n, uint32_t R, uint32_t ld, float* __restrict__ Xp,
+                          const float* __restrict__ w) {
     const size_t total = (size_t)kNR * ld;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
         const uint32_t c = (uint32_t)(t / ld), k = (uint32_t)(t % ld);
-        Xp[t] = (c < R && k < n) ? X[(size_t)c * n + k] : 0.f;
+        Xp[t] = (c < R && k < n) ? X[(size_t)c * n + k] * (w ? w[k] : 1.0f) : 0.f;
     }
 }
 
@@ -297,7 +303,7 @@ template <int NRC>
 __global__ void __launch_bounds__((kNConsumers + 1) * 32, 2)
     k_resid_stream(const float* __restrict__ F, uint32_t n, uint32_t ld, const float* __restrict__ Xp,
                    const float* __restrict__ X, const float* __restrict__ E, const float4* __restrict__ rho,
-                   uint32_t R, float* r, double* nrm, uint32_t* err) {
+                   uint32_t R, float* r, double* nrm, uint32_t* err, const float* __restrict__ inv_a) {
     extern __shared__ __align__(128) uint8_t s_raw[];
     float* stage = reinterpret_cast<float*>(s_raw);
     uint64_t* full = reinterpret_cast<uint64_t*>(s_raw + kNStages * kNStageBytes);
@@ -412,7 +418,7 @@ __global__ void __launch_bounds__((kNConsumers + 1) * 32, 2)
             const float4 rh = rho[i];
             const int chn = c % 3;
             const float rr = chn == 0 ? rh.x : (chn == 1 ? rh.y : rh.z);
-            const float v = E[(size_t)c * n + i] + rr * mine - X[(size_t)c * n + i];
+            const float v = E[(size_t)c * n + i] + rr * (mine * (inv_a ? inv_a[i] : 1.0f)) - X[(size_t)c * n + i];
             r[(size_t)c * n + i] = v;
             sq = (double)v * (double)v;
         }
@@ -430,7 +436,8 @@ __global__ void __launch_bounds__((kNConsumers + 1) * 32, 2)
 size_t sgemm_resid_scratch_floats(uint32_t R, uint32_t ld) { return R <= (uint32_t)kNR ? (size_t)kNR * ld : 0; }
 
 void launch_sgemm_resid(const float* F, uint32_t n, uint32_t ld, const float* X, const float* E, const float4* rho,
-                        uint32_t R, float* r, double* nrm, float* scratch, uint32_t* err, cudaStream_t s) {
+                        uint32_t R, float* r, double* nrm, float* scratch, uint32_t* err, cudaStream_t s,
+                        const float* w, const float* inv_a) {
     if (R <= (uint32_t)kNR) {
         static const cudaError_t attr3 =
             cudaFuncSetAttribute(k_resid_stream<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNSmem);
@@ -438,14 +445,14 @@ void launch_sgemm_resid(const float* F, uint32_t n, uint32_t ld, const float* X,
             cudaFuncSetAttribute(k_resid_stream<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNSmem);
         (void)attr3;  // a failure shows as the launch error below
         (void)attr4;
-        k_pad_rhs<<<152 * 2, 256, 0, s>>>(X, n, R, ld, scratch);
+        k_pad_rhs<<<152 * 2, 256, 0, s>>>(X, n, R, ld, scratch, w);
         const dim3 grid((n + kNRows - 1) / kNRows), block((kNConsumers + 1) * 32);
-        if (R <= 3) k_resid_stream<3><<<grid, block, kNSmem, s>>>(F, n, ld, scratch, X, E, rho, R, r, nrm, err);
-        else k_resid_stream<4><<<grid, block, kNSmem, s>>>(F, n, ld, scratch, X, E, rho, R, r, nrm, err);
+        if (R <= 3) k_resid_stream<3><<<grid, block, kNSmem, s>>>(F, n, ld, scratch, X, E, rho, R, r, nrm, err, inv_a);
+        else k_resid_stream<4><<<grid, block, kNSmem, s>>>(F, n, ld, scratch, X, E, rho, R, r, nrm, err, inv_a);
         return;
     }
     dim3 grid((n + kRBM - 1) / kRBM, (R + kRBN - 1) / kRBN);
-    k_sgemm_resid<<<grid, 256, 0, s>>>(F, n, ld, X, E, rho, R, r, nrm);
+    k_sgemm_resid<<<grid, 256, 0, s>>>(F, n, ld, X, E, rho, R, r, nrm, w, inv_a);
 }
 
 // ---------------------------------------------------------------------------
@@ -509,19 +516,60 @@ void launch_shoot_resid(const float* F, uint32_t n, uint32_t ld, const float* X,
     k_shoot_resid<<<152 * 4, 256, 0, s>>>(acc, X, E, rho, area, n, R, r);
 }
 
-// BF16 transposed copy of a column-major N x R block: Xt[c][j] (ld columns, zero padded).
+// BF16 transposed copy of a column-major N x R block: Xt[c][j] (ld columns, zero padded),
+// each value multiplied by w[j] when weights are given.
 __global__ void k_pack_bf16(const float* __restrict__ X, uint32_t n, uint32_t R, uint32_t ld, __nv_bfloat16* Xt,
-                            uint32_t Rpad) {
+                            uint32_t Rpad, const float* __restrict__ w) {
     const size_t total = (size_t)Rpad * ld;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
         const uint32_t c = (uint32_t)(e / ld), j = (uint32_t)(e % ld);
-        Xt[e] = __float2bfloat16_rn((c < R && j < n) ? X[(size_t)c * n + j] : 0.f);
+        Xt[e] = __float2bfloat16_rn((c < R && j < n) ? X[(size_t)c * n + j] * (w ? w[j] : 1.0f) : 0.f);
     }
 }
 
 void launch_pack_bf16(const float* X, uint32_t n, uint32_t R, uint32_t ld, __nv_bfloat16* Xt, uint32_t Rpad,
-                      cudaStream_t s) {
-    k_pack_bf16<<<152 * 8, 256, 0, s>>>(X, n, R, ld, Xt, Rpad);
+                      cudaStream_t s, const float* w) {
+    k_pack_bf16<<<152 * 8, 256, 0, s>>>(X, n, R, ld, Xt, Rpad, w);
+}
+
+// ---------------------------------------------------------------------------
+// Shoot-form operands: dst[i][j] = src[j][i] for i, j < n (square n x n blocks of pitch ld),
+// zeros in dst's padding columns [n, ld).  32 x 32 tiles through shared memory: both the
+// reads and the writes are row segments.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_transpose(const T* __restrict__ src, uint32_t n, uint32_t ld, T* dst) {
+    __shared__ T tile[32][33];
+    const uint32_t j0 = blockIdx.x * 32, i0 = blockIdx.y * 32;  // dst columns j0.., rows i0..
+    const uint32_t tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (uint32_t y = ty; y < 32; y += 8) {  // src row j0 + y, columns i0 + tx
+        const uint32_t j = j0 + y, i = i0 + tx;
+        tile[y][tx] = (j < n && i < n) ? src[(size_t)j * ld + i] : T(0.0f);
+    }
+    __syncthreads();
+    for (uint32_t y = ty; y < 32; y += 8) {
+        const uint32_t i = i0 + y, j = j0 + tx;
+        if (i < n && j < ld) dst[(size_t)i * ld + j] = tile[tx][y];
+    }
+}
+
+// inv_a_i = 1 / A_i (0 for a degenerate patch), w_i = s_i A_i (the BF16 rows' scale times the area).
+__global__ void k_shoot_weights(const float* __restrict__ area, const float* __restrict__ scale, uint32_t n,
+                                float* __restrict__ inv_a, float* __restrict__ w) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float a = area[i];
+        inv_a[i] = a > 0.f ? 1.0f / a : 0.f;
+        w[i] = scale[i] * a;
+    }
+}
+
+void launch_shoot_form(uint32_t n, uint32_t ld, const float* F32, float* F32T, const __nv_bfloat16* F16,
+                       __nv_bfloat16* F16T, const float* area, const float* scale, float* inv_a, float* w,
+                       cudaStream_t s) {
+    const dim3 grid(ld / 32 + (ld % 32 != 0), (n + 31) / 32);
+    if (F32 && F32T) k_transpose<float><<<grid, 256, 0, s>>>(F32, n, ld, F32T);
+    k_transpose<__nv_bfloat16><<<grid, 256, 0, s>>>(F16, n, ld, F16T);
+    k_shoot_weights<<<(n + 255) / 256, 256, 0, s>>>(area, scale, n, inv_a, w);
 }
 
 __global__ void k_axpy(float* __restrict__ y, const float* __restrict__ x, size_t total) {
@@ -706,6 +754,7 @@ __global__ void __launch_bounds__(256, 2) k_gemm_tc(const __grid_constant__ CUte
             const uint32_t row = m0 + (uint32_t)(wq * 32 + lane);
             const bool live = row < ep.n;
             const float sc = (live && ep.scale) ? ep.scale[row] : 1.0f;
+            const float ws = (live && ep.wscale) ? ep.wscale[row] : 1.0f;
             float4 rh = make_float4(0, 0, 0, 0);
             if (live && ep.mode == 1) rh = ep.rho[row];
 #pragma unroll 1
@@ -747,7 +796,7 @@ __global__ void __launch_bounds__(256, 2) k_gemm_tc(const __grid_constant__ CUte
                         y = ep.resid[(size_t)c * ep.n + row] + rr * y;
                     }
                     ep.out[(size_t)c * ep.n + row] = y;
-                    if (ep.out16) ep.out16[(size_t)c * ep.ld16 + row] = __float2bfloat16_rn(y);
+                    if (ep.out16) ep.out16[(size_t)c * ep.ld16 + row] = __float2bfloat16_rn(y * ws);
                 }
             }
         }
@@ -823,7 +872,7 @@ __global__ void k_tc_finalize(TcEpilogue ep) {
             y = ep.resid[(size_t)c * ep.n + row] + rr * y;
         }
         ep.out[(size_t)c * ep.n + row] = y;
-        if (ep.out16) ep.out16[(size_t)c * ep.ld16 + row] = __float2bfloat16_rn(y);
+        if (ep.out16) ep.out16[(size_t)c * ep.ld16 + row] = __float2bfloat16_rn(ep.wscale ? y * ep.wscale[row] : y);
     }
 }
 

@@ -5,7 +5,8 @@
 //   1. dense capture: one hemicube per patch (camera, setup, bins, raster + exact reduction,
 //      FP32 / BF16 rows) -- the same kernels as rad_dense_capture;
 //   2. emission E (3 column-major RHS) from the uploaded unshot energy, and its norms;
-//   3. first-shot direct light rho o (F E) by the streaming residual kernel;
+//   3. first-shot direct light rho o (M E) by the streaming residual kernel (M = F, or in the
+//      shoot form the reciprocity operator (M X)_i = sum_j F_ji A_j X_j / A_i);
 //   4. the warm-start features of every patch and the network's forward pass (both on the
 //      device), decoded into the guess B0 = E + s * expm1(clip(y, 0, 30));
 //   5. the residual of the guess and a check kernel, then a conditional WHILE node whose body
@@ -279,15 +280,14 @@ void enqueue_refinement(const Scene& sc, uint32_t sweeps, double tol, uint32_t m
     if (sweeps == 0) {
         cudaMemcpyAsync(sc.dd, sc.dr, 4 * nr, cudaMemcpyDeviceToDevice, s);
     } else {
-        launch_pack_bf16(sc.dr, n, R, ld, sc.d16[0], sc.Rpad, s);
+        ctx_dense_pack(c, sc.dr, R, sc.d16[0], sc.Rpad, s);
         int cur = 0;
         for (uint32_t k = 0; k < sweeps; k++) {
             TcEpilogue ep{};
+            const __nv_bfloat16* M = ctx_dense_sweep(c, ep);
             ep.mode = 1;
             ep.n = n;
             ep.R = R;
-            ep.scale = c->d_scale;
-            ep.rho = c->d_rho;
             ep.resid = sc.dr;
             ep.out = sc.dd;
             ep.out16 = sc.d16[cur ^ 1];
@@ -295,13 +295,13 @@ void enqueue_refinement(const Scene& sc, uint32_t sweeps, double tol, uint32_t m
             ep.err = &sc.dsd->err;
             ep.partial = sc.dpart;
             ep.ksplit = sc.ksplit;
-            launch_gemm_tc(c->d_F16, n, ld, sc.d16[cur], sc.Rpad, ep, s);
+            launch_gemm_tc(M, n, ld, sc.d16[cur], sc.Rpad, ep, s);
             cur ^= 1;
         }
     }
     launch_axpy(sc.dB, sc.dd, nr, s);
     cudaMemsetAsync(sc.dnrm, 0, 8 * R, s);
-    launch_sgemm_resid(c->d_F32, n, ld, sc.dB, sc.dE, c->d_rho, R, sc.dr, sc.dnrm, sc.dxp, &sc.dsd->err, s);
+    ctx_dense_resid(c, sc.dB, sc.dE, R, sc.dr, sc.dnrm, sc.dxp, &sc.dsd->err, s);
     k_mg_check<<<1, 1, 0, s>>>(sc.dnrm, sc.dsd, tol, max_outer, handle);
 }
 
@@ -334,8 +334,10 @@ int rad_multi_gather_destroy(rad_multi_gather* m) {
 }
 
 int rad_multi_gather_create(rad_ctx* const* ctxs, uint32_t count, const rad_mlp* mlp, const double* feature_dirs,
-                            double tol, uint32_t max_outer, uint32_t sweeps, rad_multi_gather** out) {
+                            double tol, uint32_t max_outer, uint32_t sweeps, uint32_t flags,
+                            rad_multi_gather** out) {
     if (!ctxs || count == 0 || !out || !(tol > 0) || sweeps > 64) return RAD_E_INVALID;
+    if (flags & ~RAD_DENSE_SHOOT_FORM) return RAD_E_INVALID;
     if (mlp && !feature_dirs) return RAD_E_INVALID;
     *out = nullptr;
     const int dev = ctxs[0]->cfg.device;
@@ -366,7 +368,7 @@ int rad_multi_gather_create(rad_ctx* const* ctxs, uint32_t count, const rad_mlp*
         Scene& sc = m->scenes[i];
         rad_ctx* c = ctxs[i];
         sc.c = c;
-        int rc = ctx_dense_alloc(c, true);
+        int rc = ctx_dense_alloc(c, true, (flags & RAD_DENSE_SHOOT_FORM) != 0);
         if (rc) return bail(rc);
         sc.n = c->n;
         sc.ld = c->dense_ld;
@@ -420,7 +422,7 @@ int rad_multi_gather_create(rad_ctx* const* ctxs, uint32_t count, const rad_mlp*
         k_mg_emission<<<1, 256, 0, s>>>(c->d_rad, n, sc.dE, sc.dsd);
         if (mlp) {
             cudaMemsetAsync(sc.dnrm, 0, 8 * 3, s);
-            launch_sgemm_resid(c->d_F32, n, ld, sc.dE, sc.dE, c->d_rho, 3, sc.ddir, sc.dnrm, sc.dxp, &sc.dsd->err, s);
+            ctx_dense_resid(c, sc.dE, sc.dE, 3, sc.ddir, sc.dnrm, sc.dxp, &sc.dsd->err, s);
             k_mg_stats<<<1, 256, 0, s>>>(c->d_verts, sc.ddir, n, sc.dsd);
             k_mg_features<<<(n + 127) / 128, 128, 0, s>>>(c->d_verts, c->d_rho, sc.dE, sc.ddir, n, fb, sc.dsd, sc.dX);
             mlp_forward_device(mlp, sc.dX, n, sc.dact0, sc.dact1, sc.dY, s);
@@ -439,7 +441,7 @@ int rad_multi_gather_create(rad_ctx* const* ctxs, uint32_t count, const rad_mlp*
              cudaGraphConditionalHandleCreate(&handle, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
         if (!ok) break;
         cudaMemsetAsync(sc.dnrm, 0, 8 * 3, s);
-        launch_sgemm_resid(c->d_F32, n, ld, sc.dB, sc.dE, c->d_rho, 3, sc.dr, sc.dnrm, sc.dxp, &sc.dsd->err, s);
+        ctx_dense_resid(c, sc.dB, sc.dE, 3, sc.dr, sc.dnrm, sc.dxp, &sc.dsd->err, s);
         k_mg_check<<<1, 1, 0, s>>>(sc.dnrm, sc.dsd, tol, max_outer, handle);
         ok = cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &ndeps) == cudaSuccess;
         if (!ok) break;

@@ -73,6 +73,18 @@ static void free_batch(BatchBuf& bb) {
     bb.has_items = false;
 }
 
+static void free_dense(rad_ctx* c) {
+    dfree(c->d_F32);
+    dfree(c->d_F16);
+    dfree(c->d_scale);
+    dfree(c->d_F32T);
+    dfree(c->d_F16T);
+    dfree(c->d_inv_area);
+    dfree(c->d_wT);
+    c->dense_ready = false;
+    c->dense_shoot = false;
+}
+
 static uint32_t tri_cap_per_hemi(const rad_ctx* c) {
     return c->cfg.tri_capacity ? c->cfg.tri_capacity : 3u * c->n + 4096u;
 }
@@ -351,9 +363,7 @@ int rad_destroy(rad_ctx* c) {
     dfree(c->d_state);
     dfree(c->d_aux);
     dfree(c->d_rows);
-    dfree(c->d_F32);
-    dfree(c->d_F16);
-    dfree(c->d_scale);
+    free_dense(c);
     if (c->h_flag) cudaFreeHost(c->h_flag);
     dfree(c->d_f3);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -397,10 +407,7 @@ int rad_upload_scene(rad_ctx* c, const float* vertices, const int32_t* indices, 
     drop_graph(c);
     free_batch(c->shoot);
     free_batch(c->aux);
-    dfree(c->d_F32);
-    dfree(c->d_F16);
-    dfree(c->d_scale);
-    c->dense_ready = false;
+    free_dense(c);
     dfree(c->d_verts);
     dfree(c->d_color);
     dfree(c->d_rho);
@@ -819,17 +826,21 @@ int rad_autotune(rad_ctx* c, uint32_t flags, rad_tuning* out) {
 
 uint32_t ctx_dense_chunk(const rad_ctx* c) { return std::min<uint32_t>(128, c->n); }
 
-int ctx_dense_alloc(rad_ctx* c, bool fp32) {
+int ctx_dense_alloc(rad_ctx* c, bool fp32, bool shoot) {
     if (!c->n) return fail(c, RAD_E_STATE, "no scene uploaded");
     const uint32_t n = c->n, ld = (n + 63u) & ~63u;
-    dfree(c->d_F32);
-    dfree(c->d_F16);
-    dfree(c->d_scale);
-    c->dense_ready = false;
+    free_dense(c);
     c->dense_ld = ld;
+    c->dense_shoot = shoot;
     RAD_CUDA(c, cudaMalloc(&c->d_F16, sizeof(__nv_bfloat16) * (size_t)n * ld));
     RAD_CUDA(c, cudaMalloc(&c->d_scale, sizeof(float) * n));
     if (fp32) RAD_CUDA(c, cudaMalloc(&c->d_F32, sizeof(float) * (size_t)n * ld));
+    if (shoot) {
+        RAD_CUDA(c, cudaMalloc(&c->d_F16T, sizeof(__nv_bfloat16) * (size_t)n * ld));
+        if (fp32) RAD_CUDA(c, cudaMalloc(&c->d_F32T, sizeof(float) * (size_t)n * ld));
+        RAD_CUDA(c, cudaMalloc(&c->d_inv_area, sizeof(float) * n));
+        RAD_CUDA(c, cudaMalloc(&c->d_wT, sizeof(float) * n));
+    }
     const uint32_t chunk = ctx_dense_chunk(c);
     int rc = alloc_batch(c, c->aux, chunk, false);
     if (rc) return rc;
@@ -860,13 +871,48 @@ void ctx_enqueue_dense_capture(rad_ctx* c, const uint32_t* d_ids, cudaStream_t s
         launch_raster(c->geo, b, c->d_fftab, c->d_aux, false, true, s);
         launch_dense_rows(b.Fq, cnt, n, c->dense_ld, first, c->d_F32, c->d_F16, c->d_scale, s);
     }
+    if (c->dense_shoot)
+        launch_shoot_form(n, c->dense_ld, c->d_F32, c->d_F32T, c->d_F16, c->d_F16T, c->d_area, c->d_scale,
+                          c->d_inv_area, c->d_wT, s);
+}
+
+void ctx_dense_resid(const rad_ctx* c, const float* X, const float* E, uint32_t R, float* r, double* nrm,
+                     float* scratch, uint32_t* err, cudaStream_t s) {
+    if (c->dense_shoot)
+        launch_sgemm_resid(c->d_F32T, c->n, c->dense_ld, X, E, c->d_rho, R, r, nrm, scratch, err, s, c->d_area,
+                           c->d_inv_area);
+    else
+        launch_sgemm_resid(c->d_F32, c->n, c->dense_ld, X, E, c->d_rho, R, r, nrm, scratch, err, s);
+}
+
+void ctx_dense_pack(const rad_ctx* c, const float* X, uint32_t R, __nv_bfloat16* Xt, uint32_t Rpad,
+                    cudaStream_t s) {
+    launch_pack_bf16(X, c->n, R, c->dense_ld, Xt, Rpad, s, c->dense_shoot ? c->d_wT : nullptr);
+}
+
+// Gather form: the rows are F_ij / s_i, so the sweep multiplies by s_i.  Shoot form: the
+// transposed rows are F_ji / s_j and the right-hand side carries s_j A_j, so the sweep
+// divides by A_i and the BF16 copy of the update is multiplied by s_i A_i for the next sweep.
+const __nv_bfloat16* ctx_dense_sweep(const rad_ctx* c, TcEpilogue& ep) {
+    ep.rho = c->d_rho;
+    if (c->dense_shoot) {
+        ep.scale = c->d_inv_area;
+        ep.wscale = c->d_wT;
+        return c->d_F16T;
+    }
+    ep.scale = c->d_scale;
+    ep.wscale = nullptr;
+    return c->d_F16;
 }
 
 extern "C" {
 
 int rad_dense_capture(rad_ctx* c, uint32_t flags, double* device_ms) {
     if (!c) return RAD_E_INVALID;
-    int rc = ctx_dense_alloc(c, (flags & RAD_DENSE_FP32) != 0);
+    if (flags & ~(RAD_DENSE_FP32 | RAD_DENSE_SHOOT_FORM)) return fail(c, RAD_E_INVALID, "unknown capture flags");
+    if ((flags & RAD_DENSE_SHOOT_FORM) && c->cfg.mode != RAD_MODE_PHYS)
+        return fail(c, RAD_E_STATE, "the shoot form needs PHYS areas");
+    int rc = ctx_dense_alloc(c, (flags & RAD_DENSE_FP32) != 0, (flags & RAD_DENSE_SHOOT_FORM) != 0);
     if (rc) return rc;
     const uint32_t n = c->n;
     cudaStream_t s = c->stream;
@@ -986,7 +1032,7 @@ int rad_gather_solve(rad_ctx* c, const float* emission, uint32_t R, const float*
     for (uint32_t outer = 0;; outer++) {
         G_CUDA(cudaMemsetAsync(dnrm, 0, 8 * (size_t)R, s));
         G_CUDA(cudaEventRecord(ev[2], s));
-        launch_sgemm_resid(c->d_F32, n, ld, dB, dE, c->d_rho, R, dr, dnrm, dxp, derr, s);
+        ctx_dense_resid(c, dB, dE, R, dr, dnrm, dxp, derr, s);
         G_CUDA(cudaEventRecord(ev[3], s));
         G_CUDA(cudaGetLastError());
         G_CUDA(cudaMemcpyAsync(nrm.data(), dnrm, 8 * (size_t)R, cudaMemcpyDeviceToHost, s));
@@ -1012,16 +1058,15 @@ int rad_gather_solve(rad_ctx* c, const float* emission, uint32_t R, const float*
         if (sweeps == 0) {
             G_CUDA(cudaMemcpyAsync(dd, dr, 4 * nr, cudaMemcpyDeviceToDevice, s));
         } else {
-            launch_pack_bf16(dr, n, R, ld, d16[0], Rpad, s);
+            ctx_dense_pack(c, dr, R, d16[0], Rpad, s);
             G_CUDA(cudaEventRecord(ev[2], s));
             int cur = 0;
             for (uint32_t k = 0; k < sweeps; k++) {
                 TcEpilogue ep{};
+                const __nv_bfloat16* M = ctx_dense_sweep(c, ep);
                 ep.mode = 1;
                 ep.n = n;
                 ep.R = R;
-                ep.scale = c->d_scale;
-                ep.rho = c->d_rho;
                 ep.resid = dr;
                 ep.out = dd;
                 ep.out16 = d16[cur ^ 1];
@@ -1029,7 +1074,7 @@ int rad_gather_solve(rad_ctx* c, const float* emission, uint32_t R, const float*
                 ep.err = derr;
                 ep.partial = dpart;
                 ep.ksplit = ksplit;
-                if (launch_gemm_tc(c->d_F16, n, ld, d16[cur], Rpad, ep, s) != 0) {
+                if (launch_gemm_tc(M, n, ld, d16[cur], Rpad, ep, s) != 0) {
                     cleanup();
                     return fail(c, RAD_E_CUDA, "tcgen05 GEMM launch failed");
                 }
@@ -1080,7 +1125,7 @@ int rad_gather_residual(rad_ctx* c, const float* emission, uint32_t R, const flo
         cudaMemsetAsync(derr, 0, 4, c->stream);
         cudaMemcpyAsync(dE, emission, 4 * nr, cudaMemcpyHostToDevice, c->stream);
         cudaMemcpyAsync(dB, radiosity, 4 * nr, cudaMemcpyHostToDevice, c->stream);
-        launch_sgemm_resid(c->d_F32, c->n, c->dense_ld, dB, dE, c->d_rho, R, dr, nullptr, dxp, derr, c->stream);
+        ctx_dense_resid(c, dB, dE, R, dr, nullptr, dxp, derr, c->stream);
         cudaMemcpyAsync(residual, dr, 4 * nr, cudaMemcpyDeviceToHost, c->stream);
         cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, c->stream);
         if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(c->stream) != cudaSuccess)

@@ -148,7 +148,8 @@ void launch_argmax(uint32_t n, bool phys, const float4* rad, const float* area, 
 namespace rad {
 // Epilogue of k_gemm_tc for C = A Bt^T (row = A row, c = Bt row):
 //   mode 0: out[c][row] = scale[row] * acc                       (column-major, + BF16 copy)
-//   mode 1: out[c][row] = resid[c][row] + rho[row].c * (scale * acc)
+//   mode 1: out[c][row] = resid[c][row] + rho[row].c * (scale * acc); its BF16 copy holds
+//           out * wscale[row] (wscale may be null: 1)
 //   mode 2: y = max(acc + bias[c], 0): BF16 out16r[row][c] (row-major, ldr) and out16[c][row]
 //   mode 3: out[row][c] = acc + bias[c]                          (row-major FP32, stride R)
 //   mode 4: y = acc if mask[row][c] > 0 else 0 (mask BF16 row-major, ldm): BF16 as mode 2
@@ -171,21 +172,29 @@ struct TcEpilogue {
     uint32_t ldr;
     const __nv_bfloat16* mask; // mode 4, row stride ldm
     uint32_t ldm;
+    const float* wscale;       // n (mode 1, may be null)
 };
 void launch_dense_rows(unsigned long long* Fq, uint32_t count, uint32_t n, uint32_t ld, uint32_t first,
                        float* F32, __nv_bfloat16* F16, float* scale, cudaStream_t s);
-// r = E + rho o (F X) - X; R <= 4 takes the streaming kernel, which needs `scratch` of
-// sgemm_resid_scratch_floats(R, ld) floats (0 for larger R: scratch may be null) and sets
-// *err (when given) if one of its bounded pipeline waits timed out.
+// r = E + rho o (inv_a o (F (w o X))) - X (w, inv_a may be null: ones); R <= 4 takes the
+// streaming kernel, which needs `scratch` of sgemm_resid_scratch_floats(R, ld) floats (0 for
+// larger R: scratch may be null) and sets *err (when given) if one of its bounded pipeline
+// waits timed out.
 size_t sgemm_resid_scratch_floats(uint32_t R, uint32_t ld);
 // One bounded mbarrier wait that nothing completes: sets *err after limit_ns.
 int launch_wait_selftest(uint32_t* err, unsigned long long limit_ns, cudaStream_t s);
 void launch_sgemm_resid(const float* F, uint32_t n, uint32_t ld, const float* X, const float* E, const float4* rho,
-                        uint32_t R, float* r, double* nrm, float* scratch, uint32_t* err, cudaStream_t s);
+                        uint32_t R, float* r, double* nrm, float* scratch, uint32_t* err, cudaStream_t s,
+                        const float* w = nullptr, const float* inv_a = nullptr);
 void launch_shoot_resid(const float* F, uint32_t n, uint32_t ld, const float* X, const float* E, const float4* rho,
                         const float* area, uint32_t R, double* acc, float* r, cudaStream_t s);
 void launch_pack_bf16(const float* X, uint32_t n, uint32_t R, uint32_t ld, __nv_bfloat16* Xt, uint32_t Rpad,
-                      cudaStream_t s);
+                      cudaStream_t s, const float* w = nullptr);
+// Shoot-form operands from the captured rows: F32T / F16T = transposes (F32 may be null),
+// inv_a = 1 / A, w = scale o A.
+void launch_shoot_form(uint32_t n, uint32_t ld, const float* F32, float* F32T, const __nv_bfloat16* F16,
+                       __nv_bfloat16* F16T, const float* area, const float* scale, float* inv_a, float* w,
+                       cudaStream_t s);
 void launch_axpy(float* y, const float* x, size_t total, cudaStream_t s);
 int launch_gemm_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv_bfloat16* Bt, uint32_t Rpad,
                    const TcEpilogue& ep, cudaStream_t s);

@@ -11,6 +11,9 @@ features of a patch to its converged radiosity.  Features, per scene:
   16-31 sin / cos of 2*pi*(p . b_k) for 8 fixed random directions b_k (Fourier features)
 Target: log1p(max(B - E, 0) / s); the guess is B0 = E + s * expm1(max(y, 0)).
 The prediction only seeds rad_gather_solve, which still iterates to its tolerance.
+
+The solves run in the shoot form (``FORM``): the gather converges to the fixed point of the
+progressive shooter, so the network learns, and seeds, the plain solver's answer.
 """
 from __future__ import annotations
 
@@ -22,6 +25,9 @@ import numpy as np
 from . import _lib, scenes
 
 _FOURIER = np.random.default_rng(1234).normal(0.0, 2.0, (8, 3)).astype(np.float64)
+
+# The system the training targets solve and the warm start seeds (see Solver.dense_capture).
+FORM = "shoot"
 
 # The network trained on solver-generated scenes by ``bench.py --workload learned
 # --save-weights`` (its training set and evaluation are recorded in the file's metadata).
@@ -88,12 +94,12 @@ def decode(scene: dict, direct: np.ndarray, Y: np.ndarray) -> np.ndarray:
     return (E + scale_of(direct) * np.expm1(y)).astype(np.float32)
 
 
-def capture(scene: dict, W: int = 128) -> "_lib.Solver":
-    """A PHYS solver with the scene's dense form factors captured (FP32 + BF16)."""
+def capture(scene: dict, W: int = 128, form: str = FORM) -> "_lib.Solver":
+    """A PHYS solver with the scene's dense form factors captured (FP32 + BF16) in `form`."""
     s = _lib.Solver(hemicube_side=W, hemicubes_count=16, mode=_lib.MODE_PHYS)
     s.upload(scene["vertices"], scene["color"], scene["radiosity"], scene["illumination"],
              reflectance=scene["reflectance"])
-    s.dense_capture(keep_fp32=True)
+    s.dense_capture(keep_fp32=True, form=form)
     return s
 
 
@@ -103,7 +109,7 @@ def emission_block(scene: dict) -> np.ndarray:
 
 
 def direct_light(solver: "_lib.Solver", E: np.ndarray) -> np.ndarray:
-    """First-shot direct light rho o (F E) as N x 3."""
+    """First-shot direct light rho o (M E) as N x 3 (M the captured form's operator)."""
     return solver.gather_residual(E, E).T.astype(np.float64)
 
 
@@ -163,13 +169,13 @@ def generated(specs, workers: int = 0):
 
 
 def training_set(n_scenes: int, seed: int = 0, patches=(2000, 6000), W: int = 128, tol: float = 1e-6,
-                 kinds=("cornell",), sample: int | None = None, workers: int = 0):
+                 kinds=("cornell",), sample: int | None = None, workers: int = 0, form: str = FORM):
     """Solver-generated (X, T) pairs: each scene of scene_specs is captured at hemicube side W
-    and solved by rad_gather_solve to `tol`; `sample` keeps at most that many random patches
-    per scene (a seeded choice)."""
+    and solved by rad_gather_solve in `form` to `tol`; `sample` keeps at most that many random
+    patches per scene (a seeded choice)."""
     Xs, Ts = [], []
     for k, sc in enumerate(generated(scene_specs(n_scenes, seed, patches, kinds), workers)):
-        with capture(sc, W) as s:
+        with capture(sc, W, form) as s:
             E = emission_block(sc)
             B, _ = s.gather(E, tol=tol, max_outer=80, sweeps=8)
             d = direct_light(s, E)
