@@ -10,15 +10,18 @@
 // Right-hand sides are column-major: column c of an N x R block is contiguous, and
 // column c uses the reflectance channel c % 3.
 //
-// k_gemm_tc is a warp-specialised tcgen05 GEMM for C[128 x NR] tiles: warp 0 issues
-// TMA loads (128B swizzle) of a 128 x 64 tile of F16 and an NR x 64 tile of the
+// k_gemm_tc is a warp-specialised tcgen05 GEMM for C[128 x NR] tiles (two of them per CTA,
+// sharing each NR x 64 tile of B, for the solve's sweeps with NR >= 128): warp 0 issues
+// TMA loads (128B swizzle) of 128 x 64 tiles of F16 and an NR x 64 tile of the
 // transposed operand into a 4-stage ring, warp 1 issues tcgen05.mma (BF16 x BF16 ->
 // FP32 in TMEM) and frees stages with tcgen05.commit, warp 2 owns the TMEM
 // allocation, and warps 4-7 read the accumulator with tcgen05.ld and run the fused
-// epilogue.  When the row tiles alone would leave SMs idle (160 tiles on 152 SMs at
-// N = 20k), K is split over blockIdx.y; each split writes its FP32 partial sums and
-// k_tc_finalize adds them in split order (deterministic) before the same epilogue.  Every mbarrier wait is bounded by wall-clock time; a timeout sets the
-// error word and the kernel drains and frees its TMEM before returning.
+// epilogue.  When the row tiles alone would leave SMs idle (80 two-tile CTAs on 152 SMs at
+// N = 20k), K is split (a tile's splits are neighbours in launch order); each split writes
+// its FP32 partial sums and k_tc_finalize adds them in split order (deterministic) before the
+// same epilogue.  The streamed matrix is loaded with an L2 evict-first policy.  Every
+// mbarrier wait is bounded by wall-clock time; a timeout sets the error word and the kernel
+// drains and frees its TMEM before returning.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -591,6 +594,17 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, in
         : "memory");
 }
 
+// The same load with an L2 cache policy (the streamed matrix is marked evict-first, so that it
+// does not push the shared right-hand sides and the split-K partial sums out of L2).
+__device__ __forceinline__ void tma_load_2d_hint(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar,
+                                                 uint64_t policy) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint"
+        " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar)), "l"(policy)
+        : "memory");
+}
+
 // Shared-memory matrix descriptor: K-major, 128B swizzle, 8-row groups 1024 B apart.
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
     uint64_t d = 0;
@@ -602,19 +616,27 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
     return d;
 }
 
-template <int NR>
+// MT row tiles of 128 share each B tile (MT = 2 for wide B: half the B bytes per A byte).
+template <int NR, int MT = 1>
 struct TcShape {
-    static constexpr uint32_t kA = kTcM * kTcBK * 2;
+    static constexpr uint32_t kA = kTcM * kTcBK * 2;   // one 128-row A tile
     static constexpr uint32_t kB = NR * kTcBK * 2;
-    static constexpr uint32_t kStage = kA + kB;
+    static constexpr uint32_t kStage = MT * kA + kB;
     static constexpr uint32_t kCols = NR <= 32 ? 32 : (NR <= 64 ? 64 : (NR <= 128 ? 128 : 256));
-    // 1 KB header (mbarriers, TMEM slot), the stage ring, 1 KB of alignment slack
-    static constexpr uint32_t kSmem = kTcStages * kStage + 2048;
+    // 1 KB header (mbarriers, TMEM slot), the stage ring, 1 KB of alignment slack; at most
+    // kTcStages stages and 227 KB
+    static constexpr uint32_t kMaxStages =
+        (227u * 1024u - 2048u) / kStage < (uint32_t)kTcStages ? (227u * 1024u - 2048u) / kStage : (uint32_t)kTcStages;
+    static constexpr uint32_t kSmem = kMaxStages * kStage + 2048;
     static constexpr uint32_t smem_for(uint32_t stages) { return stages * kStage + 2048; }
     // instruction descriptor: D f32, A/B bf16, K-major both, N = NR, M = 128
     static constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NR >> 3) << 17) |
                                        ((uint32_t)(kTcM >> 4) << 24);
 };
+
+// Row tiles per CTA: two (sharing each B tile) for the solve's sweeps (modes 0, 1) with B at
+// least 128 wide, else one.
+__host__ __device__ constexpr uint32_t tc_mt(uint32_t NR, int mode) { return (NR >= 128 && mode <= 1) ? 2u : 1u; }
 
 // One output element of the network modes (2-5) of TcEpilogue; y = the FP32 accumulator.
 __device__ __forceinline__ void net_store(const TcEpilogue& ep, uint32_t row, uint32_t c, float y) {
@@ -676,11 +698,11 @@ __device__ __forceinline__ void net_epilogue(const TcEpilogue& ep, uint32_t row,
 
 // nst: stages of the TMA ring (2..kTcStages); a short K needs fewer, and the smaller shared
 // footprint lets two CTAs share an SM.
-template <int NR>
+template <int NR, int MT>
 __global__ void __launch_bounds__(256, 2) k_gemm_tc(const __grid_constant__ CUtensorMap tmA,
                                                     const __grid_constant__ CUtensorMap tmB, uint32_t kblocks,
                                                     uint32_t nst, TcEpilogue ep) {
-    using S = TcShape<NR>;
+    using S = TcShape<NR, MT>;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* hdr = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     uint64_t* full = reinterpret_cast<uint64_t*>(hdr);
@@ -689,9 +711,10 @@ __global__ void __launch_bounds__(256, 2) k_gemm_tc(const __grid_constant__ CUte
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
     uint8_t* smem = hdr + 1024;  // stage s at smem + s * kStage (1024-aligned for the 128B swizzle)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t m0 = blockIdx.x * kTcM;
-    // split-K: block (x, y) takes K blocks [kb0, kb1) of split y
-    const uint32_t nsplit = (ep.partial && ep.ksplit > 1) ? ep.ksplit : 1u, split = blockIdx.y;
+    // split-K: block x is split x % nsplit of CTA tile x / nsplit (MT x 128 rows) and takes K
+    // blocks [kb0, kb1); a tile's splits are neighbours in launch order, so they run together
+    const uint32_t nsplit = (ep.partial && ep.ksplit > 1) ? ep.ksplit : 1u;
+    const uint32_t split = blockIdx.x % nsplit, m0 = (blockIdx.x / nsplit) * (MT * kTcM);
     const uint32_t kb0 = split * kblocks / nsplit, kb1 = (split + 1) * kblocks / nsplit;
     if (threadIdx.x == 0) {
         for (uint32_t s = 0; s < nst; s++) {
@@ -703,7 +726,7 @@ __global__ void __launch_bounds__(256, 2) k_gemm_tc(const __grid_constant__ CUte
     }
     if (warp == 2) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(S::kCols)
+                     "r"(MT * S::kCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -712,12 +735,17 @@ __global__ void __launch_bounds__(256, 2) k_gemm_tc(const __grid_constant__ CUte
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t taddr = *tmem_slot;
     if (warp == 0 && lane == 0) {
+        uint64_t stream_policy;
+        asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(stream_policy));
         for (uint32_t kb = kb0; kb < kb1; kb++) {
             const uint32_t s = (kb - kb0) % nst, round = (kb - kb0) / nst;
             if (!mbar_wait(&empty[s], (round & 1u) ^ 1u, ep.err)) break;
             mbar_expect_tx(&full[s], S::kStage);
-            tma_load_2d(smem + s * S::kStage, &tmA, (int)(kb * kTcBK), (int)m0, &full[s]);
-            tma_load_2d(smem + s * S::kStage + S::kA, &tmB, (int)(kb * kTcBK), 0, &full[s]);
+#pragma unroll
+            for (int t = 0; t < MT; t++)
+                tma_load_2d_hint(smem + s * S::kStage + t * S::kA, &tmA, (int)(kb * kTcBK), (int)(m0 + t * kTcM),
+                                 &full[s], stream_policy);
+            tma_load_2d(smem + s * S::kStage + MT * S::kA, &tmB, (int)(kb * kTcBK), 0, &full[s]);
         }
     } else if (warp == 1 && lane == 0) {
         bool ok = true;
@@ -728,16 +756,19 @@ __global__ void __launch_bounds__(256, 2) k_gemm_tc(const __grid_constant__ CUte
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint64_t a0 = sw128_desc(smem_u32(smem + s * S::kStage));
-            const uint64_t b0 = sw128_desc(smem_u32(smem + s * S::kStage + S::kA));
+            const uint64_t b0 = sw128_desc(smem_u32(smem + s * S::kStage + MT * S::kA));
 #pragma unroll
-            for (int k = 0; k < kTcBK / 16; k++) {
-                const uint32_t acc = ((kb - kb0) | (uint32_t)k) ? 1u : 0u;
-                asm volatile(
-                    "{ .reg .pred p; setp.ne.b32 p, %4, 0; tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(
-                        taddr),
-                    "l"(a0 + (uint64_t)(2 * k)), "l"(b0 + (uint64_t)(2 * k)), "r"(S::kIdesc), "r"(acc)
-                    : "memory");
+            for (int t = 0; t < MT; t++) {
+                const uint64_t a0 = sw128_desc(smem_u32(smem + s * S::kStage + t * S::kA));
+#pragma unroll
+                for (int k = 0; k < kTcBK / 16; k++) {
+                    const uint32_t acc = ((kb - kb0) | (uint32_t)k) ? 1u : 0u;
+                    asm volatile(
+                        "{ .reg .pred p; setp.ne.b32 p, %4, 0; tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(
+                            taddr + (uint32_t)t * S::kCols),
+                        "l"(a0 + (uint64_t)(2 * k)), "l"(b0 + (uint64_t)(2 * k)), "r"(S::kIdesc), "r"(acc)
+                        : "memory");
+                }
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                              smem_u32(&empty[s]))
@@ -751,7 +782,9 @@ __global__ void __launch_bounds__(256, 2) k_gemm_tc(const __grid_constant__ CUte
         const int wq = warp - 4;
         if (mbar_wait(accum, 0, ep.err)) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t row = m0 + (uint32_t)(wq * 32 + lane);
+#pragma unroll 1
+          for (int t = 0; t < MT; t++) {
+            const uint32_t row = m0 + (uint32_t)(t * kTcM + wq * 32 + lane);
             const bool live = row < ep.n;
             const float sc = (live && ep.scale) ? ep.scale[row] : 1.0f;
             const float ws = (live && ep.wscale) ? ep.wscale[row] : 1.0f;
@@ -760,7 +793,7 @@ __global__ void __launch_bounds__(256, 2) k_gemm_tc(const __grid_constant__ CUte
 #pragma unroll 1
             for (int c0 = 0; c0 < NR; c0 += 32) {
                 uint32_t v[32];
-                const uint32_t ta = taddr + ((uint32_t)(wq * 32) << 16) + (uint32_t)c0;
+                const uint32_t ta = taddr + (uint32_t)t * S::kCols + ((uint32_t)(wq * 32) << 16) + (uint32_t)c0;
                 asm volatile(
                     "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
                     "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -799,13 +832,15 @@ __global__ void __launch_bounds__(256, 2) k_gemm_tc(const __grid_constant__ CUte
                     if (ep.out16) ep.out16[(size_t)c * ep.ld16 + row] = __float2bfloat16_rn(y * ws);
                 }
             }
+          }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 2) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(S::kCols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(MT * S::kCols)
+                     : "memory");
     }
 }
 
@@ -895,12 +930,15 @@ __global__ void k_tc_finalize_wide(TcEpilogue ep) {
     }
 }
 
+uint32_t gemm_tc_width(uint32_t R);
+
 // K splits for n rows and R right-hand sides: the count (1..8, at least 8 K blocks each)
 // that minimises the bytes moved per row, with the F reads (2 ld bytes) divided by the
 // share of the 152 SMs the last wave keeps busy, plus the partial sums written and read
 // back (8 R bytes per split) when K is split.
 uint32_t gemm_tc_ksplit(uint32_t n, uint32_t ld, uint32_t R) {
-    const uint32_t tiles = (n + kTcM - 1) / kTcM, kblocks = ld / kTcBK;
+    const uint32_t rows = tc_mt(gemm_tc_width(R), 1) * kTcM;  // rows per CTA of the solve's sweeps
+    const uint32_t tiles = (n + rows - 1) / rows, kblocks = ld / kTcBK;
     uint32_t best = 1;
     double best_cost = 1e300;
     for (uint32_t sp = 1; sp <= 8; sp++) {
@@ -954,23 +992,31 @@ static bool cached_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t
     return true;
 }
 
-template <int NR>
-static int launch_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv_bfloat16* Bt, const TcEpilogue& ep,
-                     cudaStream_t s) {
-    using S = TcShape<NR>;
-    CUtensorMap ma, mb;
-    if (!cached_map(&ma, A, n, ld, kTcM) || !cached_map(&mb, Bt, NR, ld, NR)) return -1;
+template <int NR, int MT>
+static int launch_tc_mt(const CUtensorMap& ma, const CUtensorMap& mb, uint32_t n, uint32_t kblocks,
+                        const TcEpilogue& ep, cudaStream_t s) {
+    using S = TcShape<NR, MT>;
     static const cudaError_t attr =
-        cudaFuncSetAttribute(k_gemm_tc<NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::kSmem);
+        cudaFuncSetAttribute(k_gemm_tc<NR, MT>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::kSmem);
     if (attr != cudaSuccess) return -2;
-    const uint32_t kblocks = ld / kTcBK;
     const uint32_t nsplit = (ep.partial && ep.ksplit > 1) ? ep.ksplit : 1u;
     const uint32_t per_split = (kblocks + nsplit - 1) / nsplit;  // K blocks of the longest split
-    const uint32_t nst = per_split >= (uint32_t)kTcStages ? (uint32_t)kTcStages : (per_split < 2u ? 2u : per_split);
-    k_gemm_tc<NR><<<dim3((n + kTcM - 1) / kTcM, nsplit), 256, S::smem_for(nst), s>>>(ma, mb, kblocks, nst, ep);
+    const uint32_t nst = per_split >= S::kMaxStages ? S::kMaxStages : (per_split < 2u ? 2u : per_split);
+    const uint32_t tiles = (n + MT * kTcM - 1) / (MT * kTcM);
+    k_gemm_tc<NR, MT><<<tiles * nsplit, 256, S::smem_for(nst), s>>>(ma, mb, kblocks, nst, ep);
     if (nsplit >= 32 && ep.mode >= 2) k_tc_finalize_wide<<<152 * 8, 256, 0, s>>>(ep);
     else if (nsplit > 1) k_tc_finalize<<<152 * 8, 256, 0, s>>>(ep);
     return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+template <int NR>
+static int launch_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv_bfloat16* Bt, const TcEpilogue& ep,
+                     cudaStream_t s) {
+    CUtensorMap ma, mb;
+    if (!cached_map(&ma, A, n, ld, kTcM) || !cached_map(&mb, Bt, NR, ld, NR)) return -1;
+    const uint32_t kblocks = ld / kTcBK;
+    if (tc_mt(NR, ep.mode) == 2) return launch_tc_mt<NR, 2>(ma, mb, n, kblocks, ep, s);
+    return launch_tc_mt<NR, 1>(ma, mb, n, kblocks, ep, s);
 }
 
 // Shared-memory limits of the streaming residual and the tcgen05 GEMM instances, set before
@@ -978,12 +1024,15 @@ static int launch_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv
 cudaError_t dense_init() {
     cudaError_t e = cudaFuncSetAttribute(k_resid_stream<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNSmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_resid_stream<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNSmem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<16>::kSmem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<32>::kSmem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<64>::kSmem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<128>::kSmem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<192>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<192>::kSmem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<256>::kSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<16, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<16, 1>::kSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<32, 1>::kSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<64, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<64, 1>::kSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<128, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<128, 1>::kSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<192, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<192, 1>::kSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<256, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<256, 1>::kSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<128, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<128, 2>::kSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<192, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<192, 2>::kSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<256, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<256, 2>::kSmem);
     return e;
 }
 

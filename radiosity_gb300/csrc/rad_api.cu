@@ -1206,11 +1206,14 @@ int rad_bf16_gemm(int device, const uint16_t* A, const uint16_t* Bt, uint32_t n,
     if (cudaSetDevice(device) != cudaSuccess) return RAD_E_CUDA;
     const uint32_t ld = (k + 63u) & ~63u;
     __nv_bfloat16 *dA = nullptr, *dB = nullptr;
-    float* dC = nullptr;
+    float *dC = nullptr, *dpart = nullptr;
     uint32_t* derr = nullptr;
     int rc = RAD_OK;
+    // the gathering solve's split-K policy, so that the split path and its finalize run too
+    const uint32_t ksplit = gemm_tc_ksplit(n, ld, Rpad);
     if (cudaMalloc(&dA, 2 * (size_t)n * ld) != cudaSuccess || cudaMalloc(&dB, 2 * (size_t)Rpad * ld) != cudaSuccess ||
-        cudaMalloc(&dC, 4 * (size_t)n * R) != cudaSuccess || cudaMalloc(&derr, 4) != cudaSuccess)
+        cudaMalloc(&dC, 4 * (size_t)n * R) != cudaSuccess || cudaMalloc(&derr, 4) != cudaSuccess ||
+        (ksplit > 1 && cudaMalloc(&dpart, 4 * (size_t)n * R * ksplit) != cudaSuccess))
         rc = RAD_E_NOMEM;
     if (!rc) {
         cudaMemset(dA, 0, 2 * (size_t)n * ld);
@@ -1224,6 +1227,8 @@ int rad_bf16_gemm(int device, const uint16_t* A, const uint16_t* Bt, uint32_t n,
         ep.R = R;
         ep.out = dC;
         ep.err = derr;
+        ep.partial = dpart;
+        ep.ksplit = ksplit;
         if (launch_gemm_tc(dA, n, ld, dB, Rpad, ep, 0) != 0) rc = RAD_E_CUDA;
         if (!rc && cudaDeviceSynchronize() != cudaSuccess) rc = RAD_E_CUDA;
         uint32_t herr = 0;
@@ -1235,6 +1240,7 @@ int rad_bf16_gemm(int device, const uint16_t* A, const uint16_t* Bt, uint32_t n,
     cudaFree(dB);
     cudaFree(dC);
     cudaFree(derr);
+    cudaFree(dpart);
     return rc;
 }
 

@@ -22,17 +22,23 @@ def _bf16_val(bits):
     return (bits.astype(np.uint32) << 16).view(np.float32)
 
 
-@pytest.mark.parametrize("n,k,R", [(128, 64, 16), (200, 130, 3), (300, 257, 40), (513, 1000, 192), (256, 640, 256)])
+@pytest.mark.parametrize("n,k,R", [(128, 64, 16), (200, 130, 3), (300, 257, 40), (513, 1000, 192), (256, 640, 256),
+                                   (1000, 4000, 3), (700, 2500, 70), (2000, 3000, 192)])
 def test_bf16_gemm_tcgen05(lib, n, k, R):
+    """The gathering solve's stream-K sweep kernel on host arrays.  The last three shapes give
+    CTAs ranges that end inside tiles (2-5 partial tiles per tile, added by the fixup pass)."""
     rng = np.random.default_rng(n + k + R)
     A = _bf16_bits(rng.uniform(-1, 1, (n, k)).astype(np.float32))
     B = _bf16_bits(rng.uniform(-1, 1, (R, k)).astype(np.float32))
     C = lib.bf16_gemm(A, B)
+    C2 = lib.bf16_gemm(A, B)
+    assert np.array_equal(C.view(np.uint32), C2.view(np.uint32))  # deterministic
     a = _bf16_val(A).astype(np.float64)
     b = _bf16_val(B).astype(np.float64)
     ref = (a @ b.T).T
     bound = (np.abs(a) @ np.abs(b).T).T
-    assert np.all(np.abs(C - ref) <= 1e-5 * bound + 1e-30)
+    tol = 1e-5 if k <= 1024 else 3e-5  # FP32 accumulation over k terms
+    assert np.all(np.abs(C - ref) <= tol * bound + 1e-30)
 
 
 @pytest.fixture(scope="module")
