@@ -82,101 +82,182 @@ void launch_dense_rows(unsigned long long* Fq, uint32_t count, uint32_t n, uint3
 // FP32 residual GEMM: r[c][i] = E[c][i] + rho_i[c%3] * sum_j F[i][j] X[c][j] - X[c][i]
 // (with weights w and inv_a: the sum is over F[i][j] w_j X[c][j] and is multiplied by inv_a_i;
 // the shoot form passes the transposed rows, w = A and inv_a = 1 / A)
-// 128 (rows) x 64 (columns) tiles, 16-deep k slabs staged in shared memory (the next
-// slab's global loads are issued before the current slab's FMAs), 8x4 outputs per thread.
-// Every 64 k the FP32 partial sums are added to a (hi, lo) pair with Knuth's TwoSum, so the
-// sum over N ~ 20k terms carries the rounding of 64-term partials instead of growing like
-// sqrt(N) * eps: the refinement's FP32 residual then agrees with an FP64 evaluation to well
-// below the 1e-6 tolerance.  Column norms: nrm[c] += r^2 (FP64 atomics).  Entries of F at
-// columns >= n (the row padding up to ld) are never read as data.
+// 128 (rows) x 64 (columns) tiles, 128 threads with 8 x 8 outputs each (four FMAs per
+// shared-memory word loaded), 16-deep k slabs double-buffered in shared memory, the next
+// slab's global loads in flight during the current slab's FMAs, one barrier per slab.
+// Compensated sum: every 64 k the thread's FP32 chunk sums are added to their high parts (one
+// word per output, in shared memory) with Knuth's TwoSum, and the rounding error of that add
+// starts the next chunk, so the sum over N ~ 20k terms carries the rounding of 64-term
+// partials instead of growing like sqrt(N) * eps: the refinement's FP32 residual then agrees
+// with an FP64 evaluation to well below the 1e-6 tolerance.  Column norms: nrm[c] += r^2
+// (FP64 atomics).  Entries of F at columns >= n (the row padding up to ld) are never read.
 // ---------------------------------------------------------------------------
-constexpr int kRBM = 128, kRBN = 64, kRBK = 16, kRComp = 4;  // kRComp slabs between TwoSums
+constexpr int kRBM = 128, kRBN = 64, kRBK = 16, kRComp = 4, kRThreads = 128;
+constexpr int kRAs = kRBK * (kRBM + 4), kRBs = kRBK * (kRBN + 4);   // one buffer, floats
+constexpr int kRSmem = (2 * kRAs + 2 * kRBs + kRBM * kRBN) * 4;     // 58,368 B
 
-__global__ void __launch_bounds__(256) k_sgemm_resid(const float* __restrict__ F, uint32_t n, uint32_t ld,
-                                                     const float* __restrict__ X, const float* __restrict__ E,
-                                                     const float4* __restrict__ rho, uint32_t R, float* r,
-                                                     double* nrm, const float* __restrict__ w,
-                                                     const float* __restrict__ inv_a) {
-    __shared__ __align__(16) float As[kRBK][kRBM + 4];  // As[k][i]
-    __shared__ __align__(16) float Bs[kRBK][kRBN + 4];  // Bs[k][c]
+__global__ void __launch_bounds__(kRThreads, 3) k_sgemm_resid(const float* __restrict__ F, uint32_t n, uint32_t ld,
+                                                              const float* __restrict__ X,
+                                                              const float* __restrict__ E,
+                                                              const float4* __restrict__ rho, uint32_t R, float* r,
+                                                              double* nrm, const float* __restrict__ w,
+                                                              const float* __restrict__ inv_a, uint32_t nsplit,
+                                                              float* __restrict__ part) {
+    extern __shared__ __align__(16) float s_rs[];
+    float* As = s_rs;                    // [2][kRBK][kRBM + 4], As[k][i]
+    float* Bs = As + 2 * kRAs;           // [2][kRBK][kRBN + 4], Bs[k][c]
+    float* Hs = Bs + 2 * kRBs;           // [64 outputs][128 threads]: high parts
     const uint32_t i0 = blockIdx.x * kRBM, c0 = blockIdx.y * kRBN;
-    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    // global -> register staging: A: row tid/2, 8 consecutive k; B: column tid/4, 4 consecutive k
-    const int ar = tid >> 1, ak = (tid & 1) * 8, bc = tid >> 2, bk = (tid & 3) * 4;
-    const uint32_t gi = i0 + ar, gc = c0 + bc;
-    float ra[8], rb[4];
+    const int tid = threadIdx.x, tx = tid & 7, ty = tid >> 3;  // columns tx*8.., rows ty*8..
+    // global -> register staging of one slab: A rows (tid >> 2) + 32 q, k (tid & 3) * 4 .. + 3;
+    // B columns (tid >> 2) + 32 q, the same k
+    const int lr = tid >> 2, lk = (tid & 3) * 4;
+    float4 ra[4], rb[2];
     auto load = [&](uint32_t k0) {
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            const uint32_t gk = k0 + ak + j;
-            ra[j] = (gi < n && gk < n) ? F[(size_t)gi * ld + gk] : 0.f;
+        const uint32_t k = k0 + (uint32_t)lk;
+        float4 wv = make_float4(1.f, 1.f, 1.f, 1.f);
+        if (w) {
+            wv.x = k < n ? w[k] : 0.f;
+            wv.y = k + 1 < n ? w[k + 1] : 0.f;
+            wv.z = k + 2 < n ? w[k + 2] : 0.f;
+            wv.w = k + 3 < n ? w[k + 3] : 0.f;
         }
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const uint32_t gk = k0 + bk + j;
-            rb[j] = (gc < R && gk < n) ? X[(size_t)gc * n + gk] * (w ? w[gk] : 1.0f) : 0.f;
+        for (int q = 0; q < 4; q++) {
+            const uint32_t i = i0 + (uint32_t)(lr + 32 * q);
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (i < n) {
+                const float* src = F + (size_t)i * ld + k;
+                if (k + 3 < n) v = *reinterpret_cast<const float4*>(src);  // ld % 4 == 0, k % 4 == 0
+                else {
+                    if (k < n) v.x = src[0];
+                    if (k + 1 < n) v.y = src[1];
+                    if (k + 2 < n) v.z = src[2];
+                }
+            }
+            ra[q] = v;
+        }
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const uint32_t c = c0 + (uint32_t)(lr + 32 * q);
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (c < R) {
+                const float* src = X + (size_t)c * n + k;  // column c of X: n floats, no alignment
+                if (k < n) v.x = src[0] * wv.x;
+                if (k + 1 < n) v.y = src[1] * wv.y;
+                if (k + 2 < n) v.z = src[2] * wv.z;
+                if (k + 3 < n) v.w = src[3] * wv.w;
+            }
+            rb[q] = v;
         }
     };
-    float acc[8][4], hi[8][4], lo[8][4];
+    auto store = [&](int buf) {
+        float* A = As + buf * kRAs;
+        float* B = Bs + buf * kRBs;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int i = lr + 32 * q;
+            A[(lk + 0) * (kRBM + 4) + i] = ra[q].x;
+            A[(lk + 1) * (kRBM + 4) + i] = ra[q].y;
+            A[(lk + 2) * (kRBM + 4) + i] = ra[q].z;
+            A[(lk + 3) * (kRBM + 4) + i] = ra[q].w;
+        }
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const int c = lr + 32 * q;
+            B[(lk + 0) * (kRBN + 4) + c] = rb[q].x;
+            B[(lk + 1) * (kRBN + 4) + c] = rb[q].y;
+            B[(lk + 2) * (kRBN + 4) + c] = rb[q].z;
+            B[(lk + 3) * (kRBN + 4) + c] = rb[q].w;
+        }
+    };
+    float acc[8][8];
 #pragma unroll
     for (int p = 0; p < 8; p++)
 #pragma unroll
-        for (int q = 0; q < 4; q++) acc[p][q] = hi[p][q] = lo[p][q] = 0.f;
-    load(0);
-    int slab = 0;
-    for (uint32_t k0 = 0; k0 < n; k0 += kRBK) {
-#pragma unroll
-        for (int j = 0; j < 8; j++) As[ak + j][ar] = ra[j];
-#pragma unroll
-        for (int j = 0; j < 4; j++) Bs[bk + j][bc] = rb[j];
-        __syncthreads();
-        if (k0 + kRBK < n) load(k0 + kRBK);  // in flight during the FMAs below
+        for (int q = 0; q < 8; q++) {
+            acc[p][q] = 0.f;
+            Hs[(p * 8 + q) * kRThreads + tid] = 0.f;
+        }
+    // split-K: blockIdx.z takes slabs [sl0, sl1)
+    const uint32_t nslabs = (n + kRBK - 1) / kRBK;
+    const uint32_t sl0 = blockIdx.z * nslabs / nsplit, sl1 = (blockIdx.z + 1) * nslabs / nsplit;
+    load(sl0 * kRBK);
+    store(0);
+    __syncthreads();
+    for (uint32_t sl = sl0; sl < sl1; sl++) {
+        const int cur = (int)((sl - sl0) & 1u);
+        const bool more = sl + 1 < sl1;
+        if (more) load((sl + 1) * kRBK);  // in flight during the FMAs below
+        const float* A = As + cur * kRAs + ty * 8;
+        const float* B = Bs + cur * kRBs + tx * 8;
 #pragma unroll
         for (int kk = 0; kk < kRBK; kk++) {
-            const float4 a0 = *reinterpret_cast<const float4*>(&As[kk][ty * 8]);
-            const float4 a1 = *reinterpret_cast<const float4*>(&As[kk][ty * 8 + 4]);
-            const float4 b4 = *reinterpret_cast<const float4*>(&Bs[kk][tx * 4]);
+            const float4 a0 = *reinterpret_cast<const float4*>(A + kk * (kRBM + 4));
+            const float4 a1 = *reinterpret_cast<const float4*>(A + kk * (kRBM + 4) + 4);
+            const float4 b0 = *reinterpret_cast<const float4*>(B + kk * (kRBN + 4));
+            const float4 b1 = *reinterpret_cast<const float4*>(B + kk * (kRBN + 4) + 4);
             const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-            const float bb[4] = {b4.x, b4.y, b4.z, b4.w};
+            const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
             for (int p = 0; p < 8; p++)
 #pragma unroll
-                for (int q = 0; q < 4; q++) acc[p][q] = fmaf(a[p], bb[q], acc[p][q]);
+                for (int q = 0; q < 8; q++) acc[p][q] = fmaf(a[p], bb[q], acc[p][q]);
         }
-        __syncthreads();
-        if (++slab == kRComp || k0 + kRBK >= n) {
-            slab = 0;
+        if (more) store(cur ^ 1);  // the other buffer: last read before the previous barrier
+        if ((sl + 1 - sl0) % kRComp == 0 || !more) {
 #pragma unroll
             for (int p = 0; p < 8; p++)
 #pragma unroll
-                for (int q = 0; q < 4; q++) {  // TwoSum(hi, acc): s + e == hi + acc exactly
-                    const float a = hi[p][q], b = acc[p][q];
-                    const float s = a + b, bv = s - a;
-                    lo[p][q] += (a - (s - bv)) + (b - bv);
-                    hi[p][q] = s;
-                    acc[p][q] = 0.f;
+                for (int q = 0; q < 8; q++) {  // TwoSum(hi, acc): the error starts the next chunk
+                    float* hp = Hs + (p * 8 + q) * kRThreads + tid;
+                    const float h = *hp, b = acc[p][q];
+                    const float s = h + b, bv = s - h;
+                    acc[p][q] = (h - (s - bv)) + (b - bv);
+                    *hp = s;
                 }
         }
+        __syncthreads();
+    }
+    if (nsplit > 1) {  // the split's compensated sums (hi, lo) for k_sgemm_resid_finalize
+        float* phi = part + (size_t)blockIdx.z * R * n;
+        float* plo = part + (size_t)(nsplit + blockIdx.z) * R * n;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const uint32_t c = c0 + (uint32_t)(tx * 8 + q);
+            if (c >= R) continue;
+#pragma unroll
+            for (int p = 0; p < 8; p++) {
+                const uint32_t i = i0 + (uint32_t)(ty * 8 + p);
+                if (i >= n) continue;
+                phi[(size_t)c * n + i] = Hs[(p * 8 + q) * kRThreads + tid];
+                plo[(size_t)c * n + i] = acc[p][q];
+            }
+        }
+        return;
     }
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-        const uint32_t c = c0 + tx * 4 + q;
+    for (int q = 0; q < 8; q++) {
+        const uint32_t c = c0 + (uint32_t)(tx * 8 + q);
         double part = 0;
         if (c < R) {
             const int ch = (int)(c % 3);
 #pragma unroll
             for (int p = 0; p < 8; p++) {
-                const uint32_t i = i0 + ty * 8 + p;
+                const uint32_t i = i0 + (uint32_t)(ty * 8 + p);
                 if (i >= n) continue;
                 const float4 rh = rho[i];
                 const float rr = ch == 0 ? rh.x : (ch == 1 ? rh.y : rh.z);
-                const float sum = (hi[p][q] + lo[p][q]) * (inv_a ? inv_a[i] : 1.0f);
+                const float sum = (Hs[(p * 8 + q) * kRThreads + tid] + acc[p][q]) * (inv_a ? inv_a[i] : 1.0f);
                 const float v = E[(size_t)c * n + i] + rr * sum - X[(size_t)c * n + i];
                 r[(size_t)c * n + i] = v;
                 part += (double)v * (double)v;
             }
-            if (nrm) atomicAdd(&nrm[c], part);
         }
+        // lanes with the same tx (lane ^ 8, lane ^ 16) hold the same columns
+        part += __shfl_xor_sync(0xffffffffu, part, 8);
+        part += __shfl_xor_sync(0xffffffffu, part, 16);
+        if (nrm && c < R && (threadIdx.x & 31) < 8) atomicAdd(&nrm[c], part);
     }
 }
 
@@ -436,7 +517,70 @@ __global__ void __launch_bounds__((kNConsumers + 1) * 32, 2)
     }
 }
 
-size_t sgemm_resid_scratch_floats(uint32_t R, uint32_t ld) { return R <= (uint32_t)kNR ? (size_t)kNR * ld : 0; }
+// The splits' (hi, lo) pairs added in split order with TwoSum, then the residual and the norms:
+// block (x, c) takes rows x * 256 .. + 255 of column c (one FP64 atomic per block).
+__global__ void __launch_bounds__(256) k_sgemm_resid_finalize(const float* __restrict__ part, uint32_t nsplit,
+                                                              uint32_t n, const float* __restrict__ X,
+                                                              const float* __restrict__ E,
+                                                              const float4* __restrict__ rho, uint32_t R, float* r,
+                                                              double* nrm, const float* __restrict__ inv_a) {
+    const uint32_t c = blockIdx.y, i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ double s_part[8];
+    double sq = 0.0;
+    if (i < n) {
+        const size_t at = (size_t)c * n + i, stride = (size_t)R * n;
+        float H = 0.f, L = 0.f;
+        for (uint32_t sp = 0; sp < nsplit; sp++) {
+            const float h = part[sp * stride + at], l = part[(nsplit + sp) * stride + at];
+            const float s2 = H + h, bv = s2 - H;
+            L += ((H - (s2 - bv)) + (h - bv)) + l;
+            H = s2;
+        }
+        const float4 rh = rho[i];
+        const int ch = (int)(c % 3);
+        const float rr = ch == 0 ? rh.x : (ch == 1 ? rh.y : rh.z);
+        const float sum = (H + L) * (inv_a ? inv_a[i] : 1.0f);
+        const float v = E[at] + rr * sum - X[at];
+        r[at] = v;
+        sq = (double)v * (double)v;
+    }
+    if (!nrm) return;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = sq;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < 8; k++) t += s_part[k];
+        atomicAdd(&nrm[c], t);
+    }
+}
+
+// K splits of the tiled residual (R > 4): the count (1..16, at least 32 slabs each) that
+// balances the waves of 3 CTAs per SM against the partial sums written and read back.
+static uint32_t sgemm_resid_splits(uint32_t n, uint32_t R) {
+    const uint32_t ctas = ((n + kRBM - 1) / kRBM) * ((R + kRBN - 1) / kRBN), nslabs = (n + kRBK - 1) / kRBK;
+    const double slots = 152.0 * 3.0;
+    uint32_t best = 1;
+    double best_cost = 1e300;
+    for (uint32_t sp = 1; sp <= 16; sp++) {
+        if (sp > 1 && nslabs / sp < 32) break;
+        const double work = (double)ctas * sp;
+        const double fill = work / (std::ceil(work / slots) * slots);
+        const double cost = 1.0 / fill + 60.0 * sp / (double)n;
+        if (cost < best_cost - 1e-12) {
+            best_cost = cost;
+            best = sp;
+        }
+    }
+    return best;
+}
+
+size_t sgemm_resid_scratch_floats(uint32_t R, uint32_t ld) {
+    if (R <= (uint32_t)kNR) return (size_t)kNR * ld;
+    const uint32_t sp = sgemm_resid_splits(ld, R);  // sized by ld >= n, as the launch plans it
+    return sp > 1 ? (size_t)2 * sp * R * ld : 0;
+}
 
 void launch_sgemm_resid(const float* F, uint32_t n, uint32_t ld, const float* X, const float* E, const float4* rho,
                         uint32_t R, float* r, double* nrm, float* scratch, uint32_t* err, cudaStream_t s,
@@ -454,8 +598,15 @@ void launch_sgemm_resid(const float* F, uint32_t n, uint32_t ld, const float* X,
         else k_resid_stream<4><<<grid, block, kNSmem, s>>>(F, n, ld, scratch, X, E, rho, R, r, nrm, err, inv_a);
         return;
     }
-    dim3 grid((n + kRBM - 1) / kRBM, (R + kRBN - 1) / kRBN);
-    k_sgemm_resid<<<grid, 256, 0, s>>>(F, n, ld, X, E, rho, R, r, nrm, w, inv_a);
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(k_sgemm_resid, cudaFuncAttributeMaxDynamicSharedMemorySize, kRSmem);
+    (void)attr;  // a failure shows as the launch error
+    // the splits the scratch was sized for (sgemm_resid_scratch_floats); null scratch: one split
+    const uint32_t sp = scratch ? sgemm_resid_splits(ld, R) : 1u;
+    dim3 grid((n + kRBM - 1) / kRBM, (R + kRBN - 1) / kRBN, sp);
+    k_sgemm_resid<<<grid, kRThreads, kRSmem, s>>>(F, n, ld, X, E, rho, R, r, nrm, w, inv_a, sp, scratch);
+    if (sp > 1)
+        k_sgemm_resid_finalize<<<dim3((n + 255) / 256, R), 256, 0, s>>>(scratch, sp, n, X, E, rho, R, r, nrm, inv_a);
 }
 
 // ---------------------------------------------------------------------------
@@ -1023,6 +1174,7 @@ static int launch_tc(const __nv_bfloat16* A, uint32_t n, uint32_t ld, const __nv
 // the first launch (and so before any stream capture that contains them).
 cudaError_t dense_init() {
     cudaError_t e = cudaFuncSetAttribute(k_resid_stream<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sgemm_resid, cudaFuncAttributeMaxDynamicSharedMemorySize, kRSmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_resid_stream<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kNSmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<16, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<16, 1>::kSmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcShape<32, 1>::kSmem);

@@ -176,10 +176,11 @@ struct TcEpilogue {
 };
 void launch_dense_rows(unsigned long long* Fq, uint32_t count, uint32_t n, uint32_t ld, uint32_t first,
                        float* F32, __nv_bfloat16* F16, float* scale, cudaStream_t s);
-// r = E + rho o (inv_a o (F (w o X))) - X (w, inv_a may be null: ones); R <= 4 takes the
-// streaming kernel, which needs `scratch` of sgemm_resid_scratch_floats(R, ld) floats (0 for
-// larger R: scratch may be null) and sets *err (when given) if one of its bounded pipeline
-// waits timed out.
+// r = E + rho o (inv_a o (F (w o X))) - X (w, inv_a may be null: ones), `scratch` holding
+// sgemm_resid_scratch_floats(R, ld) floats.  R <= 4 takes the streaming kernel (scratch: the
+// padded right-hand sides), which sets *err (when given) if one of its bounded pipeline waits
+// timed out; larger R the tiled kernel (scratch: its split-K partial sums; when it is 0 or
+// null the tiled kernel runs unsplit).
 size_t sgemm_resid_scratch_floats(uint32_t R, uint32_t ld);
 // One bounded mbarrier wait that nothing completes: sets *err after limit_ns.
 int launch_wait_selftest(uint32_t* err, unsigned long long limit_ns, cudaStream_t s);
