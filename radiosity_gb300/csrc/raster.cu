@@ -265,8 +265,7 @@ __device__ __forceinline__ void box_union(bool okA, bool okB, const int* pa, con
     }
 }
 
-// Adds one to each bin the pixel box px touches; cnt = the hemicube's bin counters
-// (the CTA's shared-memory histogram or the global counts).
+// Adds one to each bin the pixel box px touches; cnt = the hemicube's global bin counters.
 __device__ __forceinline__ void count_bins(const Geo& g, const FaceInfo& F, const int* px, uint32_t* cnt) {
     const int sh = (int)g.tile_shift;  // boxes lie inside the scissor: offsets are >= 0
     const int c0 = (px[0] - F.sc[0]) >> sh, c1 = (px[1] - F.sc[0]) >> sh;
@@ -289,14 +288,15 @@ __device__ __forceinline__ void count_bins_warp(const Geo& g, const Batch& b, ui
         r0 = (px[2] - F.sc[1]) >> sh;
         r1 = (px[3] - F.sc[1]) >> sh;
     }
-    uint32_t* cnt = b.bin_count + (size_t)hi * g.nb + F.bin_base;
+    uint32_t* cnt = b.bin_count + (size_t)hi * g.nb;
     const bool single = on && c0 == c1 && r0 == r1;
-    const uint32_t key = single ? (uint32_t)(r0 * F.bins_x + c0) : 0xFFFFFFFFu;
+    // the hemicube-wide bin index: the lanes of a warp may draw different faces
+    const uint32_t key = single ? (uint32_t)(F.bin_base + r0 * F.bins_x + c0) : 0xFFFFFFFFu;
     const unsigned grp = __match_any_sync(0xffffffffu, key);
     if (single && (threadIdx.x & 31) == (unsigned)(__ffs(grp) - 1)) atomicAdd(&cnt[key], (uint32_t)__popc(grp));
     if (on && !single)
         for (int r = r0; r <= r1; r++)
-            for (int c = c0; c <= c1; c++) atomicAdd(&cnt[r * F.bins_x + c], 1u);
+            for (int c = c0; c <= c1; c++) atomicAdd(&cnt[F.bin_base + r * F.bins_x + c], 1u);
 }
 
 // Snap one clip-space vertex to 24.8 fixed-point window coordinates; false when w <= 0.
@@ -383,8 +383,6 @@ __device__ __forceinline__ void load_quad(const float* verts, uint32_t p, float*
     q[8] = c.x; q[9] = c.y; q[10] = c.z; q[11] = c.w;
 }
 
-constexpr uint32_t kSetupHistBins = 4096;  // 16 KB of shared memory at most
-
 // Thread per (hemicube, patch) in three phases:
 //  1. tangent-plane cull and the exact per-face test -> a 5-bit mask of faces to draw;
 //  2. warp compaction of the (patch, face) items;
@@ -399,19 +397,14 @@ __global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* _
     __shared__ float s_mvp[5 * 16];
     __shared__ float s_fr[8];
     __shared__ uint8_t s_items[4][32 * 5];  // (lane << 3) | face
-    __shared__ uint32_t s_clipq[128 * 5];   // items that need clipping: (patch << 3) | face
-    __shared__ uint32_t s_nclip;
-    // per-CTA bin histogram (when the hemicube has <= kSetupHistBins bins): shared-memory
-    // atomics per triangle, one global add per touched bin at the end
-    extern __shared__ uint32_t s_hist[];
-    const bool use_hist = g.nb <= kSetupHistBins;
-    uint32_t* gcnt = b.bin_count + (size_t)hi * g.nb;
-    uint32_t* cnt = use_hist ? s_hist : gcnt;
+    __shared__ uint32_t s_clipq[4][32 * 5]; // per warp: items that need clipping, (patch << 3) | face
+    __shared__ uint32_t s_nclip[4];
+    // bin counts go straight to the hemicube's global counters (warp-aggregated for the
+    // records that touch one bin): no shared histogram, so no barrier before its flush
+    uint32_t* cnt = b.bin_count + (size_t)hi * g.nb;
     for (int i = threadIdx.x; i < 5 * 16; i += blockDim.x) s_mvp[i] = b.mvp[(size_t)hi * 80 + i];
     if (threadIdx.x < 8) s_fr[threadIdx.x] = b.frame[(size_t)hi * 8 + threadIdx.x];
-    if (threadIdx.x == 0) s_nclip = 0;
-    if (use_hist)
-        for (uint32_t i = threadIdx.x; i < g.nb; i += blockDim.x) s_hist[i] = 0;
+    if (lane == 0) s_nclip[warp] = 0;
     __syncthreads();
     // 1. cull + face mask
     uint32_t mask = 0;
@@ -501,8 +494,8 @@ __global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* _
         }
         const bool clipq =
             has && (needs_clip(cv[0]) || needs_clip(cv[1]) || needs_clip(cv[2]) || needs_clip(cv[3]));
-        const uint32_t qpos = warp_alloc(&s_nclip, clipq ? 1u : 0u);
-        if (clipq) s_clipq[qpos] = (pp << 3) | (uint32_t)f;
+        const uint32_t qpos = warp_alloc(&s_nclip[warp], clipq ? 1u : 0u);
+        if (clipq) s_clipq[warp][qpos] = (pp << 3) | (uint32_t)f;
         SV sv[4];
         int pa[4], pb[4], px[4];
         bool okA = false, okB = false;
@@ -523,23 +516,19 @@ __global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* _
             else rec_write(sv, okA, okB, pa, pb, pp, f, &b.tris[(size_t)hi * b.tri_cap_h + base]);
             box_union(okA, okB, pa, pb, px);
         }
-        if (use_hist) {
-            if (written) count_bins(g, F, px, cnt);
-        } else {
-            count_bins_warp(g, b, hi, F, px, written);
-        }
+        count_bins_warp(g, b, hi, F, px, written);
     }
-    // queued clip items, 32 per warp: each triangle is clipped and its fan packed two
-    // triangles per record
-    __syncthreads();
-    const uint32_t nclip = s_nclip;
-    for (uint32_t r = warp * 32; r < nclip; r += blockDim.x) {  // warp-uniform trip count
+    // the warp's queued clip items, 32 at a time (no CTA barrier: warps finish on their own):
+    // each triangle is clipped and its fan packed two triangles per record
+    __syncwarp();
+    const uint32_t nclip = s_nclip[warp];
+    for (uint32_t r = 0; r < nclip; r += 32) {  // warp-uniform trip count
         const bool has = r + lane < nclip;
         uint32_t pp = 0;
         int f = 0;
         float4 cv[4];
         if (has) {
-            const uint32_t it = s_clipq[r + lane];
+            const uint32_t it = s_clipq[warp][r + lane];
             pp = it >> 3;
             f = (int)(it & 7u);
             float q[12];
@@ -563,17 +552,11 @@ __global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* _
             if (ncand) emit_polygon(g, b, poly, pn, base, pp, hi, f, hw, hh, vx, vy, cnt, st);  // counts its bins
         }
     }
-    if (use_hist) {
-        __syncthreads();
-        for (uint32_t i = threadIdx.x; i < g.nb; i += blockDim.x)
-            if (s_hist[i]) atomicAdd(&gcnt[i], s_hist[i]);
-    }
 }
 
 void launch_setup(const Geo& g, const Batch& b, const float* verts, DevState* st, cudaStream_t s) {
     dim3 grid((g.n + 127) / 128, b.K);
-    const size_t hist = g.nb <= kSetupHistBins ? sizeof(uint32_t) * g.nb : 0;
-    k_setup<<<grid, 128, hist, s>>>(g, b, verts, st);
+    k_setup<<<grid, 128, 0, s>>>(g, b, verts, st);
 }
 
 // ---------------------------------------------------------------------------
