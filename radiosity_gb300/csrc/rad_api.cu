@@ -235,7 +235,7 @@ static void enqueue_batch(rad_ctx* c) {
     cudaMemsetAsync(b.bin_count, 0, sizeof(uint32_t) * (size_t)b.K * c->geo.nb, s);
     launch_select(c->geo, b, c->d_rad, c->d_area, c->d_state, s);
     launch_camera(c->geo, b, c->d_verts, c->d_rad, c->d_state, s);
-    launch_setup(c->geo, b, c->d_verts, c->d_state, s);
+    launch_setup(c->geo, b, c->d_verts, c->d_gbox, c->d_state, s);
     launch_bins(c->geo, b, c->d_state, s);
     launch_raster(c->geo, b, c->d_fftab, c->d_state, false, true, s);
     launch_update(c->geo, b, c->d_color, c->d_rho, c->d_area, c->d_rad, c->d_state, s);
@@ -261,7 +261,7 @@ static int run_aux(rad_ctx* c, const uint32_t* shooters, uint32_t count, bool it
     RAD_CUDA(c, cudaMemsetAsync(b.bin_count, 0, sizeof(uint32_t) * (size_t)count * c->geo.nb, s));
     RAD_CUDA(c, cudaMemsetAsync(b.Fq, 0, sizeof(unsigned long long) * (size_t)count * c->n, s));
     launch_camera(c->geo, b, c->d_verts, c->d_rad, c->d_aux, s);
-    launch_setup(c->geo, b, c->d_verts, c->d_aux, s);
+    launch_setup(c->geo, b, c->d_verts, c->d_gbox, c->d_aux, s);
     launch_bins(c->geo, b, c->d_aux, s);
     launch_raster(c->geo, b, c->d_fftab, c->d_aux, items, fused, s);
     RAD_CUDA(c, cudaGetLastError());
@@ -355,6 +355,7 @@ int rad_destroy(rad_ctx* c) {
     dfree(c->d_rad);
     dfree(c->d_illum);
     dfree(c->d_area);
+    dfree(c->d_gbox);
     dfree(c->d_nb);
     dfree(c->d_shade);
     dfree(c->d_best);
@@ -414,6 +415,7 @@ int rad_upload_scene(rad_ctx* c, const float* vertices, const int32_t* indices, 
     dfree(c->d_rad);
     dfree(c->d_illum);
     dfree(c->d_area);
+    dfree(c->d_gbox);
     dfree(c->d_nb);
     dfree(c->d_shade);
     dfree(c->d_f3);
@@ -425,6 +427,7 @@ int rad_upload_scene(rad_ctx* c, const float* vertices, const int32_t* indices, 
     RAD_CUDA(c, cudaMalloc(&c->d_rad, sizeof(float4) * n));
     RAD_CUDA(c, cudaMalloc(&c->d_illum, sizeof(float4) * n));
     RAD_CUDA(c, cudaMalloc(&c->d_area, sizeof(float) * n));
+    RAD_CUDA(c, cudaMalloc(&c->d_gbox, sizeof(float) * 6 * (size_t)((n + 127) / 128)));
     RAD_CUDA(c, cudaMalloc(&c->d_f3, sizeof(float) * 6 * (size_t)n));
     RAD_CUDA(c, cudaMemcpyAsync(c->d_verts, vertices, sizeof(float) * 12 * (size_t)n, cudaMemcpyHostToDevice,
                                 c->stream));
@@ -434,6 +437,7 @@ int rad_upload_scene(rad_ctx* c, const float* vertices, const int32_t* indices, 
     if ((rc = upload_f3(c, c->d_rad, radiosity, n, 0))) return rc;
     if ((rc = upload_f3(c, c->d_illum, illumination, n, 1))) return rc;
     launch_areas(c->d_verts, n, c->d_area, c->stream);
+    launch_group_boxes(c->d_verts, n, c->d_gbox, c->stream);
     RAD_CUDA(c, cudaMemsetAsync(c->d_state, 0, sizeof(DevState), c->stream));
     launch_power0(c->d_rad, c->d_area, n, c->d_state, c->stream);
     RAD_CUDA(c, cudaGetLastError());
@@ -648,7 +652,7 @@ static int profile_batches(rad_ctx* c, uint32_t n_shots, double* stage_ms, rad_s
         RAD_CUDA(c, cudaEventRecord(ev[1], s));
         launch_camera(c->geo, b, c->d_verts, c->d_rad, c->d_state, s);
         RAD_CUDA(c, cudaEventRecord(ev[2], s));
-        launch_setup(c->geo, b, c->d_verts, c->d_state, s);
+        launch_setup(c->geo, b, c->d_verts, c->d_gbox, c->d_state, s);
         RAD_CUDA(c, cudaEventRecord(ev[3], s));
         launch_bins(c->geo, b, c->d_state, s);
         RAD_CUDA(c, cudaEventRecord(ev[4], s));
@@ -736,7 +740,7 @@ static int time_pipeline(rad_ctx* c, const std::vector<uint32_t>& sh, int reps, 
         RAD_CUDA(c, cudaMemsetAsync(b.bin_count, 0, sizeof(uint32_t) * (size_t)count * c->geo.nb, s));
         RAD_CUDA(c, cudaEventRecord(c->ev0, s));
         launch_camera(c->geo, b, c->d_verts, c->d_rad, c->d_aux, s);
-        launch_setup(c->geo, b, c->d_verts, c->d_aux, s);
+        launch_setup(c->geo, b, c->d_verts, c->d_gbox, c->d_aux, s);
         launch_bins(c->geo, b, c->d_aux, s);
         launch_raster(c->geo, b, c->d_fftab, c->d_aux, false, true, s);
         RAD_CUDA(c, cudaEventRecord(c->ev1, s));
@@ -866,7 +870,7 @@ void ctx_enqueue_dense_capture(rad_ctx* c, const uint32_t* d_ids, cudaStream_t s
         cudaMemsetAsync(b.tri_counts, 0, sizeof(uint32_t) * cnt, s);
         cudaMemsetAsync(b.bin_count, 0, sizeof(uint32_t) * (size_t)cnt * c->geo.nb, s);
         launch_camera(c->geo, b, c->d_verts, c->d_rad, c->d_aux, s);
-        launch_setup(c->geo, b, c->d_verts, c->d_aux, s);
+        launch_setup(c->geo, b, c->d_verts, c->d_gbox, c->d_aux, s);
         launch_bins(c->geo, b, c->d_aux, s);
         launch_raster(c->geo, b, c->d_fftab, c->d_aux, false, true, s);
         launch_dense_rows(b.Fq, cnt, n, c->dense_ld, first, c->d_F32, c->d_F16, c->d_scale, s);

@@ -28,6 +28,7 @@ struct rad_ctx {
     float4* d_rad = nullptr;
     float4* d_illum = nullptr;
     float* d_area = nullptr;
+    float* d_gbox = nullptr;       // bounding box of each group of 128 patches (k_setup's CTAs), 6 floats
     uint32_t* d_nb = nullptr;      // display neighbours, N x 8 (rad_upload_neighbours)
     float* d_shade = nullptr;      // display colour scratch, 2 x N x 12 (rad_display_colors)
     unsigned long long* d_best = nullptr;  // argmax key (rad_highest_patch)

@@ -120,7 +120,9 @@ constexpr int kUpdateBlocks = 152 * 8;
 // Launchers (raster.cu / shoot.cu).  All run on `s`.
 void launch_camera(const Geo& g, const Batch& b, const float* verts, const float4* rad, DevState* st,
                    cudaStream_t s);
-void launch_setup(const Geo& g, const Batch& b, const float* verts, DevState* st, cudaStream_t s);
+// gbox: bounding box (min xyz, max xyz) of each group of 128 patches (launch_group_boxes)
+void launch_setup(const Geo& g, const Batch& b, const float* verts, const float* gbox, DevState* st, cudaStream_t s);
+void launch_group_boxes(const float* verts, uint32_t n, float* gbox, cudaStream_t s);
 void launch_bins(const Geo& g, const Batch& b, DevState* st, cudaStream_t s);
 cudaError_t raster_init();  // per device, before the first launch_raster (dynamic shared memory limits)
 void launch_raster(const Geo& g, const Batch& b, const float* fftab, DevState* st, bool write_items,

@@ -383,12 +383,110 @@ __device__ __forceinline__ void load_quad(const float* verts, uint32_t p, float*
     q[8] = c.x; q[9] = c.y; q[10] = c.z; q[11] = c.w;
 }
 
-// Thread per (hemicube, patch) in three phases:
+// Bounding box (min xyz, max xyz) of each group of 128 consecutive patches: the patches of one
+// k_setup CTA.  One CTA per group.
+__global__ void __launch_bounds__(128) k_group_boxes(const float* __restrict__ verts, uint32_t n, float* gbox) {
+    __shared__ float s_lo[3][4], s_hi[3][4];
+    const uint32_t p = blockIdx.x * 128 + threadIdx.x;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    if (p < n)
+        for (int k = 0; k < 4; k++)
+            for (int d = 0; d < 3; d++) {
+                const float v = verts[12 * (size_t)p + 3 * k + d];
+                lo[d] = fminf(lo[d], v);
+                hi[d] = fmaxf(hi[d], v);
+            }
+    for (int d = 0; d < 3; d++)
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+            hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+        }
+    if ((threadIdx.x & 31) == 0)
+        for (int d = 0; d < 3; d++) {
+            s_lo[d][threadIdx.x >> 5] = lo[d];
+            s_hi[d][threadIdx.x >> 5] = hi[d];
+        }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int d = threadIdx.x;
+        gbox[6 * blockIdx.x + d] = fminf(fminf(s_lo[d][0], s_lo[d][1]), fminf(s_lo[d][2], s_lo[d][3]));
+        gbox[6 * blockIdx.x + 3 + d] = fmaxf(fmaxf(s_hi[d][0], s_hi[d][1]), fmaxf(s_hi[d][2], s_hi[d][3]));
+    }
+}
+
+void launch_group_boxes(const float* verts, uint32_t n, float* gbox, cudaStream_t s) {
+    k_group_boxes<<<(n + 127) / 128, 128, 0, s>>>(verts, n, gbox);
+}
+
+// Which faces the CTA's group box may touch, and whether any of it lies in front of the
+// shooter's tangent plane.  48 threads, one per (task, box corner): tasks 0-4 are the faces,
+// task 5 the tangent plane.  A face is impossible when all 8 corners lie outside one clip
+// plane, or (side faces) all outside the kept half, and the group is behind when all 8
+// corners are behind the plane; each test keeps a margin of 1e-5 of the largest sum of
+// absolute terms, far above the rounding of the per-patch tests, which use the same
+// expressions on points inside the box.  Bit 5 of the result: some corner is not behind.
+__device__ __forceinline__ uint32_t group_face_mask(const float* __restrict__ box, const float* s_mvp,
+                                                    const float* s_fr) {
+    const uint32_t t = threadIdx.x, task = t >> 3, k = t & 7;
+    const float x = box[(k & 1) ? 3 : 0], y = box[(k & 2) ? 4 : 1], z = box[(k & 4) ? 5 : 2];
+    constexpr float kEps = 1e-5f;
+    float u[7], m[7];  // value (inside when >= 0) and magnitude per test
+#pragma unroll
+    for (int j = 0; j < 7; j++) u[j] = m[j] = 0.f;
+    if (task < 5) {
+        const float* mm = s_mvp + task * 16;
+        const float cx = ((mm[0] * x + mm[4] * y) + mm[8] * z) + mm[12];
+        const float cy = ((mm[1] * x + mm[5] * y) + mm[9] * z) + mm[13];
+        const float cz = ((mm[2] * x + mm[6] * y) + mm[10] * z) + mm[14];
+        const float cw = ((mm[3] * x + mm[7] * y) + mm[11] * z) + mm[15];
+        const float ax = ((fabsf(mm[0] * x) + fabsf(mm[4] * y)) + fabsf(mm[8] * z)) + fabsf(mm[12]);
+        const float ay = ((fabsf(mm[1] * x) + fabsf(mm[5] * y)) + fabsf(mm[9] * z)) + fabsf(mm[13]);
+        const float az = ((fabsf(mm[2] * x) + fabsf(mm[6] * y)) + fabsf(mm[10] * z)) + fabsf(mm[14]);
+        const float aw = ((fabsf(mm[3] * x) + fabsf(mm[7] * y)) + fabsf(mm[11] * z)) + fabsf(mm[15]);
+        u[0] = cz + cw; m[0] = az + aw;  // near
+        u[1] = cw - cz; m[1] = az + aw;  // far
+        u[2] = cw - cx; m[2] = ax + aw;  // x <= w
+        u[3] = cw + cx; m[3] = ax + aw;  // x >= -w
+        u[4] = cw - cy; m[4] = ay + aw;  // y <= w
+        u[5] = cw + cy; m[5] = ay + aw;  // y >= -w
+        // the kept half of a side face (inside when > 0); the front face keeps everything
+        u[6] = task == 0 ? -cy : (task == 1 ? cy : (task == 2 ? cx : (task == 3 ? -cx : 1.f)));
+        m[6] = task <= 1 ? ay : (task <= 3 ? ax : 0.f);
+    } else if (task == 5) {
+        const float dx = x - s_fr[0], dy = y - s_fr[1], dz = z - s_fr[2];
+        u[0] = (dx * s_fr[3] + dy * s_fr[4]) + dz * s_fr[5];  // in front when >= 0
+        m[0] = (fabsf(dx * s_fr[3]) + fabsf(dy * s_fr[4])) + fabsf(dz * s_fr[5]);
+    }
+    // max over the 8 corners (lanes of one 8-lane group)
+#pragma unroll
+    for (int j = 0; j < 7; j++)
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            u[j] = fmaxf(u[j], __shfl_xor_sync(0xffffffffu, u[j], o));
+            m[j] = fmaxf(m[j], __shfl_xor_sync(0xffffffffu, m[j], o));
+        }
+    bool possible;
+    if (task < 5) {
+        possible = true;
+#pragma unroll
+        for (int j = 0; j < 6; j++)
+            if (u[j] < -kEps * m[j]) possible = false;  // every corner outside plane j
+        if (u[6] <= -kEps * m[6] && task < 4) possible = false;  // every corner outside the half
+    } else {
+        possible = !(u[0] < -kEps * m[0]);  // not every corner behind
+    }
+    return possible ? 1u << task : 0u;
+}
+
+// Thread per (hemicube, patch) in three phases, after a per-CTA test of the group's bounding
+// box (group_face_mask) that skips faces no patch of the group can touch and the whole CTA when
+// the group lies behind the shooter:
 //  1. tangent-plane cull and the exact per-face test -> a 5-bit mask of faces to draw;
 //  2. warp compaction of the (patch, face) items;
 //  3. the warp's items, one per lane with all lanes busy: corners again, clip or snap,
 //     records, bin counts.
-__global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* __restrict__ verts, DevState* st) {
+__global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* __restrict__ verts,
+                                                  const float* __restrict__ gbox, DevState* st) {
     if (st->stopped) return;
     const uint32_t hi = blockIdx.y;
     if (!b.valid[hi]) return;
@@ -404,8 +502,17 @@ __global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* _
     uint32_t* cnt = b.bin_count + (size_t)hi * g.nb;
     for (int i = threadIdx.x; i < 5 * 16; i += blockDim.x) s_mvp[i] = b.mvp[(size_t)hi * 80 + i];
     if (threadIdx.x < 8) s_fr[threadIdx.x] = b.frame[(size_t)hi * 8 + threadIdx.x];
+    __shared__ uint32_t s_gmask;
     if (lane == 0) s_nclip[warp] = 0;
+    if (threadIdx.x == 0) s_gmask = 0;
     __syncthreads();
+    if (threadIdx.x < 64) {  // warps 0 and 1: the group's face mask (48 of their lanes)
+        const uint32_t bit = group_face_mask(gbox + 6 * (size_t)blockIdx.x, s_mvp, s_fr);
+        if (bit && threadIdx.x < 48 && (threadIdx.x & 7) == 0) atomicOr(&s_gmask, bit);
+    }
+    __syncthreads();
+    const uint32_t gmask = s_gmask;
+    if (!(gmask & 32u)) return;  // the whole group is behind the shooter
     // 1. cull + face mask
     uint32_t mask = 0;
     if (p < g.n) {
@@ -420,6 +527,7 @@ __global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* _
         }
         if (!behind)
             for (int f = 0; f < 5; f++) {
+                if (!((gmask >> f) & 1u)) continue;  // no patch of the group can touch face f
                 // the z and w rows first: all four corners outside the near plane
                 // (z + w < 0) reject the face without the x and y rows.  The rows are the
                 // same float expressions as face_corners', and the tests below are its
@@ -554,9 +662,10 @@ __global__ void __launch_bounds__(128, 8) k_setup(Geo g, Batch b, const float* _
     }
 }
 
-void launch_setup(const Geo& g, const Batch& b, const float* verts, DevState* st, cudaStream_t s) {
+void launch_setup(const Geo& g, const Batch& b, const float* verts, const float* gbox, DevState* st,
+                  cudaStream_t s) {
     dim3 grid((g.n + 127) / 128, b.K);
-    k_setup<<<grid, 128, 0, s>>>(g, b, verts, st);
+    k_setup<<<grid, 128, 0, s>>>(g, b, verts, gbox, st);
 }
 
 // ---------------------------------------------------------------------------
