@@ -218,9 +218,12 @@ __device__ __forceinline__ bool tri_bbox(SV a, SV b, SV c, const FaceInfo& F, in
 __device__ __forceinline__ void tri_plane(SV a, SV b, SV c, float* ax, float* ay) {
     const long long area2 =
         ((long long)b.X - a.X) * ((long long)c.Y - a.Y) - ((long long)c.X - a.X) * ((long long)b.Y - a.Y);
-    float fa = (float)area2;
-    float e1x = (float)((long long)b.X - a.X), e1y = (float)((long long)b.Y - a.Y);
-    float e2x = (float)((long long)c.X - a.X), e2y = (float)((long long)c.Y - a.Y);
+    // correctly rounded either way; the 32-bit conversion serves the usual small triangle
+    float fa = (area2 >= INT32_MIN && area2 <= INT32_MAX) ? (float)(int32_t)area2 : (float)area2;
+    // the coordinate differences fit in 32 bits (|X|, |Y| < 2^28 for W <= 2048): 32-bit
+    // conversions of the same integers, off the slow 64-bit conversion path
+    float e1x = (float)(b.X - a.X), e1y = (float)(b.Y - a.Y);
+    float e2x = (float)(c.X - a.X), e2y = (float)(c.Y - a.Y);
     float d1 = b.D - a.D, d2 = c.D - a.D;
     float gx = (d1 * e2y - d2 * e1y) / fa;
     float gy = (d2 * e1x - d1 * e2x) / fa;
@@ -304,8 +307,10 @@ __device__ __forceinline__ bool snap_vertex(float4 c, float hw, float hh, float 
     if (!(c.w > 0)) return false;
     const float xd = c.x / c.w, yd = c.y / c.w;
     const float xw = (xd + 1.0f) * hw + vx, yw = (yd + 1.0f) * hh + vy;
-    o.X = (int32_t)__float2ll_rn(xw * 256.0f);
-    o.Y = (int32_t)__float2ll_rn(yw * 256.0f);
+    // inside the guard band |xw * 256| < 2^28 (W <= 2048): a 32-bit round-to-nearest-even
+    // conversion, the same value as the 64-bit one
+    o.X = __float2int_rn(xw * 256.0f);
+    o.Y = __float2int_rn(yw * 256.0f);
     o.D = 1.0f / c.w;
     return true;
 }
@@ -1204,8 +1209,8 @@ __global__ void __launch_bounds__(256, 4) k_raster(Geo g, Batch b, const float* 
                     // the planes' constant terms at the scissor origin, rebuilt with the
                     // set-up's float operations (gx = ax / 256 exactly)
                     const float d0 = __int_as_float(p.x);
-                    const float ox = (float)((long long)sx * 256 + 128 - xs.x);
-                    const float oy = (float)((long long)sy * 256 + 128 - ys.x);
+                    const float ox = (float)(sx * 256 + 128 - xs.x);  // < 2^29 in magnitude: int32
+                    const float oy = (float)(sy * 256 + 128 - ys.x);
                     const float axA = __int_as_float(p.y), axB = __int_as_float(p.z);
                     const float ayA = __int_as_float(p.w), ayB = __int_as_float(q.x);
                     const float c0A = (d0 + (axA * 0x1p-8f) * ox) + (ayA * 0x1p-8f) * oy;
