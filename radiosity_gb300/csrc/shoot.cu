@@ -407,7 +407,8 @@ void launch_select(const Geo& g, const Batch& b, const float4* rad, const float*
 // ---------------------------------------------------------------------------
 // Radiosity update (source/Main.cpp:1271-1278)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_update(Geo g, Batch b, const float4* __restrict__ color,
+constexpr int kUpdateThreads = 128;  // small blocks: 4 per SM even at N = 50k
+__global__ void __launch_bounds__(kUpdateThreads) k_update(Geo g, Batch b, const float4* __restrict__ color,
                                                 const float4* __restrict__ rho, const float* __restrict__ area,
                                                 float4* __restrict__ rad, DevState* st) {
     if (st->stopped) return;
@@ -432,7 +433,7 @@ __global__ void __launch_bounds__(256) k_update(Geo g, Batch b, const float4* __
     // The hemicubes' contributions are added in hemicube order (the float sums must match
     // the oracle's order); their exact sums are loaded kLoad at a time ahead of use, so a
     // thread keeps several independent loads in flight instead of one.
-    constexpr int kLoad = 8;
+    constexpr int kLoad = 16;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
         float4 r = rad[i];
         const float ai = g.mode ? area[i] : 0.f;
@@ -471,7 +472,7 @@ __global__ void __launch_bounds__(256) k_update(Geo g, Batch b, const float4* __
         if (g.mode != 0) acc += (double)area[i] * (((double)r.x + (double)r.y) + (double)r.z);
     }
     if (g.mode != 0) {  // FP64 partial of the unshot power after the update (residual)
-        __shared__ double red[256];
+        __shared__ double red[kUpdateThreads];
         red[threadIdx.x] = acc;
         __syncthreads();
         for (uint32_t o = blockDim.x / 2; o > 0; o >>= 1) {
@@ -483,14 +484,14 @@ __global__ void __launch_bounds__(256) k_update(Geo g, Batch b, const float4* __
 }
 
 static uint32_t update_blocks(uint32_t n) {
-    uint32_t blocks = (n + 255) / 256;
+    uint32_t blocks = (n + kUpdateThreads - 1) / kUpdateThreads;
     if (blocks > (uint32_t)kUpdateBlocks) blocks = kUpdateBlocks;
     return blocks ? blocks : 1;
 }
 
 void launch_update(const Geo& g, const Batch& b, const float4* color, const float4* rho, const float* area,
                    float4* rad, DevState* st, cudaStream_t s) {
-    k_update<<<update_blocks(g.n), 256, 0, s>>>(g, b, color, rho, area, rad, st);
+    k_update<<<update_blocks(g.n), kUpdateThreads, 0, s>>>(g, b, color, rho, area, rad, st);
 }
 
 // ---------------------------------------------------------------------------
