@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libradiosity_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["rad_api.cu", "raster.cu", "shoot.cu", "noalloc.cu", "dense.cu", "mlp.cu", "display.cu", "multi_gather.cu"]
+CU_SOURCES = ["rad_api.cu", "raster.cu", "shoot.cu", "noalloc.cu", "dense.cu", "resid.cu", "mlp.cu", "display.cu", "multi_gather.cu"]
 CPP_SOURCES = ["scene_ref.cpp"]
 
 

@@ -184,6 +184,13 @@ void launch_dense_rows(unsigned long long* Fq, uint32_t count, uint32_t n, uint3
 // timed out; larger R the tiled kernel (scratch: its split-K partial sums; when it is 0 or
 // null the tiled kernel runs unsplit).
 size_t sgemm_resid_scratch_floats(uint32_t R, uint32_t ld);
+// resid.cu: the streaming kernel of the R <= kResidStreamRhs residual (scratch: kResidStreamRhs
+// x ld floats) and its shared-memory limits (before the first launch).
+constexpr uint32_t kResidStreamRhs = 4;
+void launch_resid_stream(const float* F, uint32_t n, uint32_t ld, const float* X, const float* E, const float4* rho,
+                         uint32_t R, float* r, double* nrm, float* scratch, uint32_t* err, cudaStream_t s,
+                         const float* w, const float* inv_a);
+cudaError_t resid_stream_init();
 // One bounded mbarrier wait that nothing completes: sets *err after limit_ns.
 int launch_wait_selftest(uint32_t* err, unsigned long long limit_ns, cudaStream_t s);
 void launch_sgemm_resid(const float* F, uint32_t n, uint32_t ld, const float* X, const float* E, const float4* rho,
