@@ -108,6 +108,7 @@ static int alloc_batch(rad_ctx* c, BatchBuf& bb, uint32_t K, bool items) {
     b.tri_cap = (uint32_t)tri_cap;
     b.tri_cap_h = tri_cap_per_hemi(c);
     b.list_cap = (uint32_t)list_cap;
+    b.list_cap_h = list_cap_per_hemi(c);
     const size_t nbk = (size_t)K * c->geo.nb;
     RAD_CUDA(c, cudaMalloc(&b.shooters, sizeof(uint32_t) * K));
     RAD_CUDA(c, cudaMalloc(&b.valid, sizeof(uint32_t) * K));

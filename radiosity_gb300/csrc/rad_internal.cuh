@@ -93,6 +93,8 @@ struct Batch {
     uint32_t tri_cap;            // K * tri_cap_h
     uint32_t list_cap;
     uint32_t tri_cap_h;          // triangle records per hemicube
+    uint32_t list_cap_h;         // bin references per hemicube: hemicube h's lists are in
+                                 // [h * list_cap_h, (h + 1) * list_cap_h) of bin_list
     uint32_t* tri_counts;        // K per-hemicube record counts
     uint32_t* shooters;          // K
     uint32_t* valid;             // K

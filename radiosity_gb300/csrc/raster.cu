@@ -676,13 +676,18 @@ void launch_setup(const Geo& g, const Batch& b, const float* verts, const float*
 // ---------------------------------------------------------------------------
 // Bin lists
 // ---------------------------------------------------------------------------
-// Exclusive scan of the K * nb bin counts by one CTA in tiles of 4096: each thread takes 4
-// consecutive counts (coalesced), warps scan with shuffles, a carry links the tiles.  Also
-// clears the fill cursors and flags a bin-list overflow.
-__global__ void __launch_bounds__(1024) k_scan(Geo g, Batch b, DevState* st) {
+// Exclusive scan of each hemicube's nb bin counts, one CTA per hemicube (the hemicubes' lists
+// have separate regions of list_cap_h references), in tiles of 4 counts per thread: warps scan
+// with shuffles, a carry links the tiles.  Also clears the fill cursors and flags a bin-list
+// overflow of the hemicube.
+__global__ void __launch_bounds__(256) k_scan(Geo g, Batch b, DevState* st) {
     if (st->stopped) return;
-    const uint32_t total = b.K * g.nb;
-    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t hi = blockIdx.x, total = g.nb;
+    uint32_t* count = b.bin_count + (size_t)hi * g.nb;
+    uint32_t* offset = b.bin_offset + (size_t)hi * g.nb;
+    uint32_t* fill = b.bin_fill + (size_t)hi * g.nb;
+    const uint32_t region = hi * b.list_cap_h;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
     __shared__ uint32_t s_warp[32];
     __shared__ uint32_t s_carry;
     if (tid == 0) s_carry = 0;
@@ -691,7 +696,7 @@ __global__ void __launch_bounds__(1024) k_scan(Geo g, Batch b, DevState* st) {
         const uint32_t i0 = base + 4 * tid;
         uint32_t c[4];
 #pragma unroll
-        for (int k = 0; k < 4; k++) c[k] = i0 + k < total ? b.bin_count[i0 + k] : 0u;
+        for (int k = 0; k < 4; k++) c[k] = i0 + k < total ? count[i0 + k] : 0u;
         const uint32_t t4 = (c[0] + c[1]) + (c[2] + c[3]);
         uint32_t x = t4;  // inclusive warp scan of the threads' 4-count totals
 #pragma unroll
@@ -702,7 +707,7 @@ __global__ void __launch_bounds__(1024) k_scan(Geo g, Batch b, DevState* st) {
         if (lane == 31) s_warp[warp] = x;
         __syncthreads();
         if (warp == 0) {
-            uint32_t w = lane < (blockDim.x >> 5) ? s_warp[lane] : 0u;
+            uint32_t w = lane < nwarps ? s_warp[lane] : 0u;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
@@ -715,8 +720,8 @@ __global__ void __launch_bounds__(1024) k_scan(Geo g, Batch b, DevState* st) {
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             if (i0 + k < total) {
-                b.bin_offset[i0 + k] = run;
-                b.bin_fill[i0 + k] = 0;
+                offset[i0 + k] = region + run;
+                fill[i0 + k] = 0;
             }
             run += c[k];
         }
@@ -724,7 +729,7 @@ __global__ void __launch_bounds__(1024) k_scan(Geo g, Batch b, DevState* st) {
         if (tid == blockDim.x - 1) s_carry = run;  // the tile's end
         __syncthreads();
     }
-    if (tid == 0 && s_carry > b.list_cap) atomicOr(&st->overflow, 2u);
+    if (tid == 0 && s_carry > b.list_cap_h) atomicOr(&st->overflow, 2u);
 }
 
 __global__ void k_fill(Geo g, Batch b, DevState* st) {
@@ -783,7 +788,7 @@ __global__ void k_fill(Geo g, Batch b, DevState* st) {
 }
 
 void launch_bins(const Geo& g, const Batch& b, DevState* st, cudaStream_t s) {
-    k_scan<<<1, 1024, 0, s>>>(g, b, st);
+    k_scan<<<b.K, 256, 0, s>>>(g, b, st);
     k_fill<<<dim3(std::max(2u, (152u * 16u) / b.K), b.K), 256, 0, s>>>(g, b, st);
 }
 
