@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(1024) k_psel_final(Geo g, Batch b, DevState* s
     __shared__ uint32_t hist[256];
     __shared__ unsigned long long arr[kMaxK];
     __shared__ unsigned long long s_prefix, s_mask;
-    __shared__ uint32_t s_rem, s_cnt;
+    __shared__ uint32_t s_rem, s_cnt, s_done;
     const int t = threadIdx.x;
     const uint32_t K = b.K, n_sure = min(b.sel_ctrl[2], K), n_bnd = min(b.sel_ctrl[3], g.n);
     const uint32_t take = min(K, b.sel_ctrl[4]);
@@ -312,6 +312,7 @@ __global__ void __launch_bounds__(1024) k_psel_final(Geo g, Batch b, DevState* s
         s_mask = 0;
         s_rem = R;
         s_cnt = 0;
+        s_done = 0;
     }
     __syncthreads();
     // Boundary elements share the top 12 composite bits (their histogram bin); an
@@ -331,20 +332,40 @@ __global__ void __launch_bounds__(1024) k_psel_final(Geo g, Batch b, DevState* s
                 if ((c & pm) == pv) atomicAdd(&hist[(c >> sh) & dmask], 1u);
             }
             __syncthreads();
-            if (t == 0) {
-                uint32_t cum = 0;
+            if (t < 32) {
+                // the bin holding the rem-th largest: lane l covers bins dmask - 8l .. dmask - 8l - 7
+                // (descending); a warp scan of the lanes' totals finds the lane, which walks its bins
                 const uint32_t rem = s_rem;
-                for (int v = (int)dmask; v >= 0; v--) {
-                    if (cum + hist[v] >= rem) {
-                        s_rem = rem - cum;
-                        s_prefix = pv | ((unsigned long long)v << sh);
-                        s_mask = pm | (dmask << sh);
-                        break;
+                const int top = (int)dmask - 8 * t;
+                uint32_t local = 0;
+                for (int j = 0; j < 8; j++)
+                    if (top - j >= 0) local += hist[top - j];
+                uint32_t incl = local;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (t >= o) incl += y;
+                }
+                const uint32_t excl = incl - local;
+                if (excl < rem && rem <= incl) {
+                    uint32_t cum = excl;
+                    for (int j = 0; j < 8; j++) {
+                        const int v = top - j;
+                        if (cum + hist[v] >= rem) {
+                            s_rem = rem - cum;
+                            s_prefix = pv | ((unsigned long long)v << sh);
+                            s_mask = pm | (dmask << sh);
+                            // the bin is taken whole: the prefix with zero low digits is the
+                            // threshold that selects exactly rem elements
+                            s_done = cum + hist[v] == rem ? 1u : 0u;
+                            break;
+                        }
+                        cum += hist[v];
                     }
-                    cum += hist[v];
                 }
             }
             __syncthreads();
+            if (s_done) break;
         }
         thr = s_prefix;
     }
