@@ -380,8 +380,7 @@ int rad_set_progress(rad_ctx* ctx, uint32_t shots_done, double initial_power);
  * scratch is a fixed device array of RAD_NOALLOC_MAX_SUMS 64-bit sums (8 MiB) that every
  * GPU loading the library holds until exit, so count * n_patches must not exceed
  * RAD_NOALLOC_MAX_SUMS (else RAD_E_NOALLOC_LIMIT).  The first call on a device looks the
- * array up (make it before any stream capture); calls that overlap on the GPU race on
- * the shared array. */
+ * array up; calls that overlap on the GPU race on the shared array. */
 #define RAD_NOALLOC_MAX_SUMS (1u << 20)
 int rad_reduce_items_noalloc(const uint32_t* d_items, uint32_t count, uint32_t hemicube_side,
                              uint32_t n_patches, float* d_ff_rows, void* stream);

@@ -17,8 +17,7 @@
 // uses before accumulating, so a call never sees a previous call's contents;
 // calls that overlap on the GPU (different streams or host threads) race on it.
 // The device address of the array is looked up with cudaGetSymbolAddress once per
-// device, with that device current, on the first call made on that device; make
-// that first call before any stream capture.
+// device, with that device current, on the first call made on that device.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
