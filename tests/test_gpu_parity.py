@@ -174,6 +174,28 @@ def test_select_phys(lib, orc, room, K):
             assert np.array_equal(v, rv) and np.array_equal(i[v], ri[rv])
 
 
+@pytest.mark.parametrize("K", [33, 128])
+def test_select_phys_few_candidates(lib, orc, room, K):
+    """Fewer patches with unshot power than shooters: a zero state, three lit patches, and
+    K - 1 / K + 1 lit patches of one power (one radix bucket taken whole or in part)."""
+    rng = np.random.default_rng(300 + K)
+    n = room["n"]
+    area = orc.patch_areas(room["vertices"])
+    vals, cnt = np.unique(area, return_counts=True)
+    same = np.flatnonzero(area == vals[np.argmax(cnt)])  # patches of one area: equal powers
+    assert same.size > K + 1 and np.all(area > 0)
+    with solver(lib, room, 16, K, mode=1) as s:
+        for lit in (0, 3, K - 1, K + 1):
+            rad = np.zeros(3 * n, np.float32)
+            ids = rng.choice(n, lit, replace=False) if lit == 3 else rng.choice(same, lit, replace=False)
+            rad[3 * ids] = 1.0
+            s.set_state(radiosity=rad)
+            i, v = s.select()
+            ri, rv = orc.topk_phys(rad, area, K)
+            assert np.array_equal(v, rv) and np.array_equal(i[v], ri[rv]), lit
+            assert int(v.sum()) == min(lit, K)
+
+
 def test_shoot_ref_bit_exact_and_record_path(lib, orc, cornell):
     W, K, S = 32, 10, 25
     with solver(lib, cornell, W, K) as s:
@@ -208,6 +230,22 @@ def test_shoot_ref_runs_to_stop_rule(lib, orc, small):
                 break
         rad2, _ = s.download()
     assert done == ost.shots_done and np.array_equal(_bits(rad2), _bits(orad))
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_shoot_dark_scene(lib, orc, small, room, mode):
+    """Nothing left to shoot: the loop stops where the oracle stops, with the same states."""
+    sc = small if mode == 0 else room
+    W, K, S = 16, 8, 6
+    zero = np.zeros(3 * sc["n"], np.float32)
+    with solver(lib, sc, W, K, mode=mode) as s:
+        s.set_state(radiosity=zero, illumination=zero)
+        st = s.shoot(S)
+        rad, ill = s.download()
+    orad, oill, ost = orc.shoot(mode, W, K, sc["vertices"], sc["color"], zero, zero, S,
+                                rho=sc.get("reflectance") if mode else None)
+    assert ost.stopped == 1 and st.stopped == 1 and st.shots_done == ost.shots_done
+    assert np.array_equal(_bits(rad), _bits(orad)) and np.array_equal(_bits(ill), _bits(oill))
 
 
 def test_shoot_phys_bit_exact(lib, orc, room):
